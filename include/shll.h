@@ -1,0 +1,184 @@
+/*
+ * shll.h -- C-ABI of libshll_gb300.so, the GB300 (sm_103a) SHLL finite-volume Euler solver.
+ *
+ * The library replaces the hot path of the reference project archembaud/shll-sve-cfd: the
+ * split-flux evaluation, interface flux sum and conservative update inside the explicit time
+ * loop of base-c/base_shll.c (1D, first order), base-c/2nd_order_base_shll.c (second order;
+ * its x sweep is the 1D second-order scheme) and base-c/base_shll_2d.c (2D, first order).
+ *
+ * The reference has no library API: each solver is a program whose stages are global-state
+ * functions  void Allocate_and_Init_Memory(void), Compute_U_from_P, Compute_P_from_U,
+ * Compute_F_from_P, Update_U_from_F, Save_Results, Free_Memory  driven by main().  This header
+ * keeps those stages as calls on a context (so several problems can live in one process) and
+ * also exports the reference's own void names on a default context (shll_ref_*), so that a
+ * reference-style main() links unchanged.
+ *
+ * Conventions: every call that can fail returns int (SHLL_OK = 0, negative = error) and
+ * shll_last_error() describes the last failure of that context.  All pointers in the
+ * signatures are HOST pointers; device memory is owned by the context.  2D fields use the
+ * reference's layout, cell index = i*ny + j (y contiguous), i.e. base-c/base_shll_2d.c:94-101.
+ */
+#ifndef SHLL_GB300_H
+#define SHLL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SHLL_OK 0
+#define SHLL_ERR_ARG (-1)         /* invalid argument or parameter */
+#define SHLL_ERR_CUDA (-2)        /* CUDA runtime error (message in shll_last_error) */
+#define SHLL_ERR_STATE (-3)       /* call out of order (e.g. stage call before init) */
+#define SHLL_ERR_NOMEM (-4)       /* device or host allocation failed */
+#define SHLL_ERR_NUMERIC (-5)     /* non-positive density/temperature or NaN detected */
+#define SHLL_ERR_TIMEOUT (-6)     /* a bounded device-side wait expired */
+#define SHLL_ERR_UNSUPPORTED (-7) /* combination not implemented (e.g. stage calls in mixed mode) */
+
+/* ---- arithmetic of the time loop ---- */
+enum shll_precision {
+    /* FP64 throughout, as the reference with float replaced by double.  Multiply-adds may be
+     * fused (the only licensed difference from the CPU reference). */
+    SHLL_PREC_F64 = 0,
+    /* FP64 throughout with no fused multiply-add: bit-identical to the FP64 reference build. */
+    SHLL_PREC_F64_EXACT = 1,
+    /* The reference as published: float arrays with the double promotions its double
+     * literals and sqrt() cause, no fused multiply-add; bit-identical to base-c built by gcc
+     * on x86-64. */
+    SHLL_PREC_F32_EXACT = 2,
+    /* Split fluxes in FP32 (perturbation form about per-segment FP64 anchor states), state in
+     * FP64; per-step increments are summed in compensated FP32 for fold_steps steps and then
+     * added to the FP64 state.  fold_steps = 1 adds every step into FP64. */
+    SHLL_PREC_MIXED_F64 = 3,
+    /* Split fluxes in FP32 as above; the state is an FP32 value plus its FP32 compensation
+     * (Kahan / float-float), with no FP64 arithmetic per cell. */
+    SHLL_PREC_MIXED_KAHAN = 4
+};
+
+/* ---- initial conditions ---- */
+enum shll_ic_kind {
+    SHLL_IC_SOD = 0,         /* 1D: left state for i < x_d*nx, right state otherwise
+                                (base-c/base_shll.c:53-60 with x_d = 0.5) */
+    SHLL_IC_REF_BOX2D = 1,   /* 2D: base-c/base_shll_2d.c:92-103 (rho 1 inside (0.2,0.8)^2, 10 outside) */
+    SHLL_IC_CIRCLE2D = 2,    /* 2D: "in" state strictly inside a circle of cell centres, else "out" */
+    SHLL_IC_FOUR_SHOCK2D = 3,/* 2D: base-c/2nd_order_base_shll.c:133-149 */
+    SHLL_IC_USER = 4,        /* primitives supplied later with shll_set_primitives() */
+    SHLL_IC_QUADRANTS2D = 5  /* 2D: base-omp/2nd_order_base_shll.c:147-172 ("Configuration 6") */
+};
+
+typedef struct shll_ic {
+    int kind;                      /* enum shll_ic_kind */
+    double x_d;                    /* SOD: diaphragm position as a fraction of the tube */
+    double rho_l, u_l, T_l;        /* SOD: left state; CIRCLE2D: inside state (u ignored) */
+    double rho_r, u_r, T_r;        /* SOD: right state; CIRCLE2D: outside state (u ignored) */
+    double cx, cy, radius;         /* CIRCLE2D: centre and radius in domain units */
+} shll_ic;
+
+typedef struct shll_params {
+    int dim;           /* 1 or 2 */
+    int order;         /* 1: first order, reflective walls (base_shll.c, base_shll_2d.c)
+                          2: second order, minmod slopes of the split fluxes, outflow walls
+                             (2nd_order_base_shll.c) */
+    int nx, ny;        /* cells (ny ignored in 1D); nx, ny >= 2 */
+    double gamma, R;   /* ratio of specific heats, gas constant (reference: 1.4, 1.0) */
+    double cfl;        /* kinetic CFL: DT = (cfl/(R+1)) * DX as base_shll.c:83 (reference 0.25) */
+    double lx, ly;     /* domain lengths (reference 1.0) */
+    double t_end;      /* run while time < t_end ... */
+    long n_steps;      /* ... unless n_steps > 0: then exactly n_steps steps */
+    int precision;     /* enum shll_precision */
+    int limiter;       /* order 2 only: 0 minmod (base-c), 1 MC limiter (base-omp/2nd_order_base_shll.c:316-325) */
+    double mc_alpha;   /* MC limiter alpha (base-omp: 1.25) */
+    int fold_steps;    /* MIXED_F64: steps between FP64 folds; 0 = library default */
+    int clock_f32;     /* 1: time accumulates in float as the published reference (default for
+                          F32_EXACT); 0: double, as the FP64 reference build */
+    shll_ic ic;
+} shll_params;
+
+typedef struct shll_ctx shll_ctx;
+
+/* Fills p with the reference's defaults for (dim, order): gamma 1.4, R 1, CFL 0.25, L = 1,
+ * Sod (1D), reference box (2D first order) or four-shock (2D second order) initial data,
+ * t_end 0.2 / 0.1 / 0.8 (base_shll.c:26, base_shll_2d.c:35, 2nd_order_base_shll.c:43),
+ * nx = ny = 256, precision F64. */
+void shll_params_default(shll_params* p, int dim, int order);
+
+/* Step count of the reference time loop for these parameters: time += DT (in float when
+ * clock_f32, else double) while time < t_end; or n_steps when > 0. */
+long shll_steps_for(const shll_params* p);
+
+/* Creates a context on the current CUDA device (allocates its device state). */
+int shll_create(const shll_params* p, shll_ctx** out);
+void shll_destroy(shll_ctx* ctx);
+const char* shll_last_error(const shll_ctx* ctx);
+const char* shll_status_string(int status);
+/* Binds the context's work to a cudaStream_t (NULL = the context's own stream). */
+int shll_set_stream(shll_ctx* ctx, void* cuda_stream);
+
+/* ---- the reference's stages (base-c/base_shll.c:28-177) ---- */
+/* Allocate_and_Init_Memory (:28-61): primitives from p->ic on the device.  Also computes U
+ * from P and P from U (main() :204-205), so the context is ready to step. */
+int shll_init_state(shll_ctx* ctx);
+/* Replaces the primitives (host arrays of nx*ny doubles; v ignored in 1D) and recomputes U and
+ * P as shll_init_state does. */
+int shll_set_primitives(shll_ctx* ctx, const double* rho, const double* u, const double* v,
+                        const double* T);
+int shll_compute_U_from_P(shll_ctx* ctx);   /* base_shll.c:74-85 */
+int shll_compute_P_from_U(shll_ctx* ctx);   /* base_shll.c:161-177 */
+int shll_compute_F_from_P(shll_ctx* ctx);   /* base_shll.c:130-159 (split fluxes) */
+int shll_update_U_from_F(shll_ctx* ctx);    /* base_shll.c:87-128 (stencil + update) */
+
+/* ---- fused time stepping ---- */
+/* Advances n steps (F -> update -> P per step, fused on the device). */
+int shll_step(shll_ctx* ctx, long n);
+/* The time loop of main() (base_shll.c:207-218): runs the remaining steps of
+ * shll_steps_for(p).  *steps_taken (may be NULL) receives the total steps of the context. */
+int shll_run(shll_ctx* ctx, long* steps_taken);
+long shll_steps_taken(const shll_ctx* ctx);
+
+/* ---- results (host copies) ---- */
+int shll_get_primitives(shll_ctx* ctx, double* rho, double* u, double* v, double* T);
+/* conserved planes rho, rho*u, [rho*v,] E, each nx*ny doubles, written contiguously */
+int shll_get_conserved(shll_ctx* ctx, double* planes);
+/* split-flux planes of the last shll_compute_F_from_P (fp, fm; hp, hm in 2D may be NULL) */
+int shll_get_fluxes(shll_ctx* ctx, double* fp, double* fm, double* hp, double* hm);
+/* FP64 sums over all cells of rho, rho*u, [rho*v,] E (device reduction); out has 3 or 4 */
+int shll_totals(shll_ctx* ctx, double* out);
+/* Save_Results (base_shll.c:180-192, base_shll_2d.c:322-340): text file of
+ * x [y] rho u [v] T per cell, "%e" tab-separated, x = (i+0.5)*DX in the reference's float */
+int shll_save_results(shll_ctx* ctx, const char* path);
+
+/* ---- batches of independent tubes / domains ---- */
+typedef struct shll_batch shll_batch;
+/* items: count parameter sets (all dim 1, or all dim 2, any sizes/orders/initial data);
+ * precision must be a MIXED mode or F64 for every item. */
+int shll_batch_create(const shll_params* items, int count, shll_batch** out);
+/* Runs every item to its own end (its own DT and step count). */
+int shll_batch_run(shll_batch* b);
+int shll_batch_get_primitives(shll_batch* b, int item, double* rho, double* u, double* v,
+                              double* T);
+int shll_batch_totals(shll_batch* b, int item, double* out);
+long shll_batch_cell_updates(const shll_batch* b);
+const char* shll_batch_last_error(const shll_batch* b);
+void shll_batch_destroy(shll_batch* b);
+
+/* ---- the reference's own entry points on a process-wide default context ----
+ * shll_ref_configure() chooses the problem (else base_shll.c's defaults, N = 256, F64). */
+int shll_ref_configure(const shll_params* p);
+shll_ctx* shll_ref_context(void);
+void Allocate_and_Init_Memory(void);
+void Compute_U_from_P(void);
+void Compute_P_from_U(void);
+void Compute_F_from_P(void);
+void Update_U_from_F(void);
+void Save_Results(void);
+void Free_Memory(void);
+/* DT of the default context (the reference's global float DT, base_shll.c:23) */
+double shll_ref_dt(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

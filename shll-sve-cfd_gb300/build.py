@@ -1,0 +1,73 @@
+"""Builds libshll_gb300.so (the CUDA kernels and the C-ABI of include/shll.h) for sm_103a.
+
+Each translation unit is compiled by its own nvcc process (in parallel), then linked with
+nvcc -shared.  Output: <package>/_build/libshll_gb300.so (git-ignored, rebuilt on each machine).
+"""
+import concurrent.futures
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libshll_gb300.so")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC]
+# translation units and their extra flags: -fmad=false where results must not depend on the
+# compiler's choice of fused multiply-adds (bit-exact reference arithmetic; the mixed engine,
+# whose halo recomputation must agree bit for bit with each cell's owner)
+UNITS = {
+    "capi.cu": [],
+    "plain_fast.cu": [],
+    "plain_exact.cu": ["-fmad=false"],
+    "mixed1d.cu": ["-fmad=false"],
+    "mixed2d.cu": ["-fmad=false"],
+    "reduce.cu": [],
+}
+HEADERS = ["shll_internal.h", "shll_plain.cuh", "mixed.h", "mixed_common.cuh"]
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(unit, flags, verbose):
+    src = os.path.join(CSRC, unit)
+    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(HERE, "..", "include", "shll.h")]
+    if not _stale(obj, deps):
+        return obj, ""
+    cmd = [NVCC] + COMMON + flags + ["-c", src, "-o", obj]
+    if verbose:
+        cmd += ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {unit}:\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build(verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        futs = [ex.submit(_compile, u, f, verbose) for u, f in UNITS.items()]
+        objs = []
+        for fu in futs:
+            obj, log = fu.result()
+            objs.append(obj)
+            if verbose and log:
+                print(log, file=sys.stderr)
+    if _stale(LIB, objs):
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,722 @@
+// Mixed-precision 1D SHLL engine: FP32 split fluxes in perturbation form, compensated FP32
+// accumulation, FP64 (or FP32-pair) state folded once per sweep.
+//
+// Scheme (the arithmetic of base-c/base_shll.c:87-159 and of the x sweep of
+// base-c/2nd_order_base_shll.c:203-459, re-associated as interface fluxes):
+//   * Cells are grouped in chunks (one CTA each).  Every chunk has a frame: the FP64 state U* of
+//     its centre cell at the start of the sweep and the split-flux coefficients derived from it.
+//   * A cell's split fluxes are evaluated in FP32 as deviations from the frame's
+//     (d fp = fp(U) - fp(U*), d fm likewise), using only deviations as FP32 operands, so their
+//     rounding error scales with |U - U*| instead of |U|.
+//   * The flux through interface j+1/2 is Fref(frame of cell j) + Delta_{j+1/2}; Delta uses
+//     cells j-1..j+2 expressed in that frame.  Both neighbouring cells add the same value (with
+//     opposite signs), so the scheme is conservative to rounding of the state; a cell whose left
+//     neighbour lies in another frame also adds lam*(Fref_left - Fref_own) (FP64, as an FP32 pair).
+//     Chunks recompute their neighbours' halo cells in the NEIGHBOUR's frame, so every chunk
+//     evaluates every interface bit for bit like its owner (this file is compiled with
+//     -fmad=false; fused operations are explicit).
+//   * Per step, lam*Delta terms are added to an FP32 value+compensation pair per cell (TwoSum).
+//     At the end of a sweep (fold_steps steps) the pair is added to the stored state: in FP64
+//     (SHLL_PREC_MIXED_F64) or in FP32-pair arithmetic (SHLL_PREC_MIXED_KAHAN).
+//   * A chunk is computed with a halo of order*steps cells on each side (temporal blocking), so
+//     one launch advances every chunk of every tube by a whole sweep with no inter-CTA waits.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "mixed.h"
+#include "mixed_common.cuh"
+#include "shll_internal.h"
+
+namespace {
+
+constexpr int MT = 128;       // threads per CTA
+constexpr int MC = 4;         // cells per thread
+constexpr int MW = MT * MC;   // window capacity (cells)
+
+struct TubeP {
+    long base;        // offset of cell 0 in the planes
+    int n, order, limiter;
+    int steps;        // steps of the current run
+    int par;          // buffer holding the tube's state at the start of the run
+    double gamma, R, CV, lam;
+    float alpha;
+};
+
+struct Chunk {
+    int tube;
+    int a, b;                // owned cells [a, b)
+    int ancL, ancO, ancR;    // anchor (centre) cells of the left / own / right chunk, -1 if none
+};
+
+struct Frame1 {
+    double U[3];      // anchor state
+    double F[3];      // physical flux at the anchor = fp* + fm*
+    double fpS1, fmS1;
+    AnchorCoef c;
+    float Uh[3], Ul[3];  // anchor as an FP32 pair
+};
+
+__device__ void make_frame(Frame1& f, const double U[3], const TubeP& tp) {
+    double rho = U[0], m = U[1], E = U[2];
+    double u = m / rho, e = E / rho;
+    double T = (e - 0.5 * u * u) / tp.CV;
+    double a = sqrt(tp.gamma * tp.R * T);
+    double M = u / a, P = rho * tp.R * T;
+    double Z1 = 0.5 * (M + 1.0), Z2 = 0.5 * a * (1.0 - M * M), Z3 = 0.5 * (M - 1.0);
+    double F[3] = {m, m * u + P, u * (E + P)};
+    for (int k = 0; k < 3; k++) {
+        f.U[k] = U[k];
+        f.F[k] = F[k];
+        f.c.F[k] = (float)F[k];
+        f.c.Uf[k] = (float)U[k];
+        f.Uh[k] = (float)U[k];
+        f.Ul[k] = (float)(U[k] - (double)f.Uh[k]);
+    }
+    f.fpS1 = F[1] * Z1 + m * Z2;
+    f.fmS1 = -F[1] * Z3 - m * Z2;
+    f.c.rho = (float)rho; f.c.u = (float)u; f.c.v = 0.f; f.c.e = (float)e; f.c.T = (float)T; f.c.a = (float)a;
+    f.c.M = (float)M; f.c.P = (float)P; f.c.Z1 = (float)Z1; f.c.Z2 = (float)Z2;
+    f.c.gR = (float)(tp.gamma * tp.R); f.c.R = (float)tp.R; f.c.cvinv = (float)(1.0 / tp.CV);
+}
+
+// reads the stored state of tube cell i as FP64 (F64 planes, or an FP32 pair)
+template <bool KAHAN>
+__device__ __forceinline__ double load_state(const void* __restrict__ hi, const float* __restrict__ lo, long idx) {
+    if (KAHAN) return (double)static_cast<const float*>(hi)[idx] + (double)lo[idx];
+    return static_cast<const double*>(hi)[idx];
+}
+
+struct SweepArgs {
+    const TubeP* tubes;
+    const Chunk* chunks;
+    void* hi[2];        // state planes of each buffer (double, or FP32 value)
+    float* lo[2];       // FP32 compensation planes (Kahan)
+    long plane;         // cells per plane (all tubes)
+    int sweep, B;
+    int* flag;
+};
+
+struct Smem1 {
+    Frame1 fr[3];
+    float sfp[3][MW], sfm[3][MW];
+    float xfp[2][3][3], xfm[2][3][3];   // [boundary][slot][comp] alternate-frame fluxes
+    float sTh[3][MW], sTl[3][MW];       // lam*Delta of interface (w, w+1), as an FP32 pair
+    float cB[2][3][2];                  // lam*(Fref_left - Fref_right) at each boundary (pair)
+    float dFr[2][3][2];                 // U*_left - U*_right at each boundary (pair)
+    float wall[2][3][2];                // constant wall terms (order 1) for cell 0 / n-1
+};
+
+template <int ORDER, bool KAHAN>
+__device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp, Smem1& S) {
+    constexpr int R_ = ORDER;  // stencil reach per step
+    Frame1* fr = S.fr;
+    auto& sfp = S.sfp; auto& sfm = S.sfm; auto& xfp = S.xfp; auto& xfm = S.xfm;
+    auto& sTh = S.sTh; auto& sTl = S.sTl; auto& cB = S.cB; auto& dFr = S.dFr; auto& wall = S.wall;
+
+    const int tid = threadIdx.x;
+    const int n = tp.n;
+    const int steps = min(A.B, tp.steps - A.sweep * A.B);
+    if (steps <= 0) return;
+    const int H = R_ * steps;
+    const int ws = max(0, ch.a - H), we = min(n, ch.b + H), L = we - ws;
+    const int pa = ch.a - ws, pb = ch.b - ws;  // frame boundaries in window coordinates
+    const int inb = (tp.par + A.sweep) & 1, outb = inb ^ 1;
+    const void* hin = A.hi[inb];
+    const float* lin = A.lo[inb];
+    const long base = tp.base;
+    const long P = A.plane;
+
+    if (L > MW) {  // host guarantees this never happens; refuse rather than overrun
+        if (tid == 0) atomicOr(A.flag, SHLL_FLAG_BADARG);
+        return;
+    }
+    // frames: 0 = left neighbour, 1 = own, 2 = right neighbour
+    if (tid < 3) {
+        int anc = tid == 0 ? ch.ancL : (tid == 1 ? ch.ancO : ch.ancR);
+        if (anc >= 0) {
+            double U[3];
+            for (int k = 0; k < 3; k++) U[k] = load_state<KAHAN>(hin, lin, k * P + base + anc);
+            make_frame(fr[tid], U, tp);
+        }
+    }
+    __syncthreads();
+    const double lam = tp.lam;
+    const float lamh = (float)lam, laml = (float)(lam - (double)lamh);
+    if (tid < 6) {
+        int bnd = tid / 3, k = tid % 3;
+        bool has = bnd == 0 ? ch.ancL >= 0 : ch.ancR >= 0;
+        int fl = bnd == 0 ? 0 : 1, frr = bnd == 0 ? 1 : 2;
+        double c = has ? lam * (fr[fl].F[k] - fr[frr].F[k]) : 0.0;
+        double d = has ? fr[fl].U[k] - fr[frr].U[k] : 0.0;
+        split2(c, cB[bnd][k][0], cB[bnd][k][1]);
+        split2(d, dFr[bnd][k][0], dFr[bnd][k][1]);
+        // order-1 reflective walls: constant parts of the wall-cell increments
+        // cell 0:   lam*F_{-1/2} - lam*Fref = (-lam F0, lam (2 fmS1 - F1), -lam F2) (+2 lam dfm1_0)
+        // cell n-1: lam*Fref - lam*F_{n-1/2} = (lam F0, lam (F1 - 2 fpS1), lam F2) (-2 lam dfp1_{n-1})
+        if (ORDER == 1) {
+            const Frame1& f = fr[1];
+            double w = bnd == 0 ? (k == 1 ? lam * (2.0 * f.fmS1 - f.F[1]) : -lam * f.F[k])
+                                : (k == 1 ? lam * (f.F[1] - 2.0 * f.fpS1) : lam * f.F[k]);
+            split2(w, wall[bnd][k][0], wall[bnd][k][1]);
+        }
+    }
+    __syncthreads();
+
+    // ---- load the window as deviations from each cell's frame ----
+    float dh[MC][3], dl[MC][3];
+#pragma unroll
+    for (int q = 0; q < MC; q++) {
+        const int w = tid * MC + q;
+        const int f = w < pa ? 0 : (w < pb ? 1 : 2);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            dh[q][k] = 0.f; dl[q][k] = 0.f;
+            if (w < L) {
+                const long idx = k * P + base + ws + w;
+                if (KAHAN) {
+                    float h = static_cast<const float*>(hin)[idx], l = lin[idx];
+                    ff_sub(h, l, fr[f].Uh[k], fr[f].Ul[k], dh[q][k], dl[q][k]);
+                } else {
+                    double d = static_cast<const double*>(hin)[idx] - fr[f].U[k];
+                    split2(d, dh[q][k], dl[q][k]);
+                }
+            }
+        }
+    }
+
+    for (int s = 0; s < steps; s++) {
+        // ---- split-flux deviations in the cell's own frame (+ alternate frames at boundaries) ----
+#pragma unroll
+        for (int q = 0; q < MC; q++) {
+            const int w = tid * MC + q;
+            if (w >= L) continue;
+            const int f = w < pa ? 0 : (w < pb ? 1 : 2);
+            float d[3], p3[3], m3[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) d[k] = __fadd_rn(dh[q][k], dl[q][k]);
+            dflux1(fr[f].c, d, p3, m3);
+#pragma unroll
+            for (int k = 0; k < 3; k++) { sfp[k][w] = p3[k]; sfm[k][w] = m3[k]; }
+            // alternate frames: boundary at pa (frames 0|1) and pb (frames 1|2)
+#pragma unroll
+            for (int bnd = 0; bnd < 2; bnd++) {
+                const int beta = bnd == 0 ? pa : pb;
+                const bool has = bnd == 0 ? ch.ancL >= 0 : ch.ancR >= 0;
+                if (!has) continue;
+                int slot = -1, g = 0;
+                float sgn = 1.f;
+                if (w == beta - 1) { slot = 0; g = bnd + 1; sgn = 1.f; }              // left cell in right frame
+                else if (w == beta || (ORDER == 2 && w == beta + 1)) { slot = 1 + (w - beta); g = bnd; sgn = -1.f; }
+                if (slot < 0) continue;
+                // deviation in frame g: d + (U*_f - U*_g) = d +/- (U*_left - U*_right)
+                float e[3], ap[3], am[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    float sh = __fadd_rn(dh[q][k], sgn * dFr[bnd][k][0]);
+                    float sl = __fadd_rn(dl[q][k], sgn * dFr[bnd][k][1]);
+                    e[k] = __fadd_rn(sh, sl);
+                }
+                dflux1(fr[g].c, e, ap, am);
+#pragma unroll
+                for (int k = 0; k < 3; k++) { xfp[bnd][slot][k] = ap[k]; xfm[bnd][slot][k] = am[k]; }
+            }
+        }
+        __syncthreads();
+        // ---- interface terms lam*Delta_{w+1/2} in the frame of cell w ----
+        auto gp = [&](int k, int c, int f) -> float {  // d fp of window cell c in frame f
+            c = max(0, min(L - 1, c));
+            int fc = c < pa ? 0 : (c < pb ? 1 : 2);
+            if (fc == f) return sfp[k][c];
+            if (f < fc) { int bnd = f; int beta = bnd == 0 ? pa : pb; int sl = 1 + (c - beta); sl = min(2, max(1, sl)); return xfp[bnd][sl][k]; }
+            int bnd = fc; return xfp[bnd][0][k];
+        };
+        auto gm = [&](int k, int c, int f) -> float {
+            c = max(0, min(L - 1, c));
+            int fc = c < pa ? 0 : (c < pb ? 1 : 2);
+            if (fc == f) return sfm[k][c];
+            if (f < fc) { int bnd = f; int beta = bnd == 0 ? pa : pb; int sl = 1 + (c - beta); sl = min(2, max(1, sl)); return xfm[bnd][sl][k]; }
+            int bnd = fc; return xfm[bnd][0][k];
+        };
+#pragma unroll
+        for (int q = 0; q < MC; q++) {
+            const int w = tid * MC + q;
+            if (w >= L - 1) continue;
+            const int i = ws + w;  // tube cell
+            const int f = w < pa ? 0 : (w < pb ? 1 : 2);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                float Dl;
+                if (ORDER == 1) {
+                    Dl = __fadd_rn(gp(k, w, f), gm(k, w + 1, f));
+                } else {
+                    float p0 = gp(k, w - 1, f), p1 = gp(k, w, f), p2 = gp(k, w + 1, f);
+                    float m1 = gm(k, w, f), m2 = gm(k, w + 1, f), m3 = gm(k, w + 2, f);
+                    float sp = (i == 0 || i == n - 1) ? 0.f : slope_f(p0, p1, p2, tp.limiter, tp.alpha);
+                    float sm = (i + 1 == n - 1) ? 0.f : slope_f(m1, m2, m3, tp.limiter, tp.alpha);
+                    Dl = __fadd_rn(__fadd_rn(__fadd_rn(p1, __fmul_rn(0.5f, sp)), m2), -__fmul_rn(0.5f, sm));
+                }
+                float th = __fmul_rn(lamh, Dl);
+                float tl = __fadd_rn(__fmaf_rn(lamh, Dl, -th), __fmul_rn(laml, Dl));
+                sTh[k][w] = th; sTl[k][w] = tl;
+            }
+        }
+        __syncthreads();
+        // ---- accumulate: lam*(F_{i-1/2} - F_{i+1/2}) per cell ----
+#pragma unroll
+        for (int q = 0; q < MC; q++) {
+            const int w = tid * MC + q;
+            if (w >= L) continue;
+            const int i = ws + w;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                float& h = dh[q][k];
+                float& l = dl[q][k];
+                if (i > 0 && w > 0) { two_sum_acc(h, l, sTh[k][w - 1]); l = __fadd_rn(l, sTl[k][w - 1]); }
+                if (i < n - 1 && w < L - 1) { two_sum_acc(h, l, -sTh[k][w]); l = __fadd_rn(l, -sTl[k][w]); }
+                if (w > 0 && (w == pa || w == pb)) {  // left neighbour in another frame
+                    const int bnd = w == pa ? 0 : 1;
+                    two_sum_acc(h, l, cB[bnd][k][0]); l = __fadd_rn(l, cB[bnd][k][1]);
+                }
+                if (i == 0 || i == n - 1) {
+                    if (ORDER == 1) {
+                        const int bnd = i == 0 ? 0 : 1;
+                        two_sum_acc(h, l, wall[bnd][k][0]); l = __fadd_rn(l, wall[bnd][k][1]);
+                        if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
+                            float v = i == 0 ? __fmul_rn(2.f, sfm[1][w]) : -__fmul_rn(2.f, sfp[1][w]);
+                            float vh = __fmul_rn(lamh, v);
+                            float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
+                            two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
+                        }
+                    } else {  // outflow: F_{-1/2} = Fref + dfp_0 + dfm_0 (and likewise at n-1)
+                        float v = __fadd_rn(sfp[k][w], sfm[k][w]);
+                        if (i == n - 1) v = -v;
+                        float vh = __fmul_rn(lamh, v);
+                        float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
+                        two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- fold the owned cells into the stored state ----
+    int bad = 0;
+    void* hout = A.hi[outb];
+    float* lout = A.lo[outb];
+#pragma unroll
+    for (int q = 0; q < MC; q++) {
+        const int w = tid * MC + q;
+        if (w < pa || w >= pb) continue;
+        double uu[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const long idx = k * P + base + ws + w;
+            if (KAHAN) {
+                float oh, ol;
+                ff_add(fr[1].Uh[k], fr[1].Ul[k], dh[q][k], dl[q][k], oh, ol);
+                static_cast<float*>(hout)[idx] = oh;
+                lout[idx] = ol;
+                uu[k] = (double)oh;
+            } else {
+                double v = fr[1].U[k] + ((double)dh[q][k] + (double)dl[q][k]);
+                static_cast<double*>(hout)[idx] = v;
+                uu[k] = v;
+            }
+        }
+        float r = (float)uu[0], m = (float)uu[1], E = (float)uu[2];
+        float eint = __fadd_rn(E, -__fmul_rn(0.5f, __fdividef(__fmul_rn(m, m), r)));
+        bad |= !(r > 0.f) || !(eint > 0.f);
+    }
+    if (bad) atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
+}
+
+template <bool KAHAN>
+__global__ void __launch_bounds__(MT) k_sweep1d(SweepArgs A) {
+    __shared__ Smem1 S;
+    const Chunk ch = A.chunks[blockIdx.x];
+    const TubeP tp = A.tubes[ch.tube];
+    if (tp.order == 2) sweep_chunk<2, KAHAN>(A, ch, tp, S);
+    else sweep_chunk<1, KAHAN>(A, ch, tp, S);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// host side
+struct MixedState {
+    int dim = 1, nitems = 0, precision = SHLL_PREC_MIXED_F64, B = 16;
+    bool kahan = false;
+    cudaStream_t stream = nullptr;
+    std::vector<shll_params> items;
+    std::vector<TubeP> tubes;          // host copy
+    std::vector<int> par;              // per tube: buffer holding its current state
+    long plane = 0;                    // cells per plane
+    void* hi[2] = {nullptr, nullptr};
+    float* lo[2] = {nullptr, nullptr};
+    TubeP* d_tubes = nullptr;
+    Chunk* d_chunks = nullptr;
+    std::vector<Chunk> chunks;         // sorted by the steps of their tube (descending)
+    int* d_flag = nullptr;
+    long cell_updates = 0;
+    // 2D engine (mixed2d.cu)
+    void* d2 = nullptr;
+};
+
+static int chunk_owned(int order, int B) { return MW - 2 * order * B; }
+
+static void build_chunks(MixedState* m) {
+    m->chunks.clear();
+    for (int t = 0; t < m->nitems; t++) {
+        const TubeP& tp = m->tubes[t];
+        const int n = tp.n;
+        if (n <= MW) {
+            m->chunks.push_back({t, 0, n, -1, n / 2, -1});
+            continue;
+        }
+        const int S = chunk_owned(tp.order, m->B);
+        const int k = (n + S - 1) / S;
+        std::vector<int> edges(k + 1);
+        for (int c = 0; c <= k; c++) edges[c] = (int)((long)n * c / k);
+        for (int c = 0; c < k; c++) {
+            int a = edges[c], b = edges[c + 1];
+            int ancL = c > 0 ? (edges[c - 1] + a) / 2 : -1;
+            int ancR = c + 1 < k ? (b + edges[c + 2]) / 2 : -1;
+            m->chunks.push_back({t, a, b, ancL, (a + b) / 2, ancR});
+        }
+    }
+}
+
+static int alloc_mixed(MixedState* m, char* err, size_t len) {
+    const size_t cells = (size_t)m->plane * 3;
+    for (int b = 0; b < 2; b++) {
+        if (cudaMalloc(&m->hi[b], cells * (m->kahan ? sizeof(float) : sizeof(double))) != cudaSuccess) {
+            snprintf(err, len, "cudaMalloc of %zu state values failed", cells);
+            return SHLL_ERR_NOMEM;
+        }
+        if (m->kahan && cudaMalloc(&m->lo[b], cells * sizeof(float)) != cudaSuccess) {
+            snprintf(err, len, "cudaMalloc of compensation planes failed");
+            return SHLL_ERR_NOMEM;
+        }
+    }
+    if (cudaMalloc(&m->d_tubes, sizeof(TubeP) * m->nitems) != cudaSuccess ||
+        cudaMalloc(&m->d_flag, sizeof(int)) != cudaSuccess || cudaMemset(m->d_flag, 0, sizeof(int)) != cudaSuccess) {
+        snprintf(err, len, "cudaMalloc of descriptors failed");
+        return SHLL_ERR_NOMEM;
+    }
+    return SHLL_OK;
+}
+
+// FP64 reference constants of one item (the reference's REAL = double values)
+static void item_consts(const shll_params& p, double* CV, double* lam, double* lamy) {
+    double R = p.R, g = p.gamma;
+    *CV = R / (g - 1.0);
+    double dx = p.lx / p.nx, dy = p.ly / (p.dim == 2 ? p.ny : 1);
+    double dt = (p.cfl / (R + 1)) * dx;
+    *lam = p.cfl / (R + 1);
+    *lamy = dt / dy;
+}
+
+MixedState* mixed2d_attach(MixedState* m, char* err, size_t len);  // mixed2d.cu
+void mixed2d_detach(MixedState* m);
+int mixed2d_load(MixedState* m, int item, const double* prim, char* err, size_t len);
+int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len);
+int mixed2d_item_conserved(MixedState* m, int item, double* planes, char* err, size_t len);
+int mixed2d_totals(MixedState* m, int item, double* out, char* err, size_t len);
+
+MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t s, char* err, size_t len) {
+    if (count <= 0 || !items) { snprintf(err, len, "empty batch"); return nullptr; }
+    MixedState* m = new MixedState();
+    m->stream = s;
+    m->nitems = count;
+    m->items.assign(items, items + count);
+    m->dim = items[0].dim;
+    m->precision = items[0].precision;
+    m->kahan = m->precision == SHLL_PREC_MIXED_KAHAN;
+    int fold = items[0].fold_steps > 0 ? items[0].fold_steps : 16;
+    for (int t = 0; t < count; t++) {
+        if (items[t].dim != m->dim || items[t].precision != m->precision) {
+            snprintf(err, len, "batch items must share dim and precision");
+            delete m;
+            return nullptr;
+        }
+        if (items[t].precision != SHLL_PREC_MIXED_F64 && items[t].precision != SHLL_PREC_MIXED_KAHAN) {
+            snprintf(err, len, "the mixed engine takes MIXED_F64 or MIXED_KAHAN items");
+            delete m;
+            return nullptr;
+        }
+    }
+    if (m->dim == 2) {
+        m->B = fold;
+        if (!mixed2d_attach(m, err, len)) { delete m; return nullptr; }
+        return m;
+    }
+    // sweep length: the fold interval, capped so that a chunk keeps at least half its window
+    m->B = std::min(fold, MW / 16);
+    long off = 0;
+    for (int t = 0; t < count; t++) {
+        const shll_params& p = items[t];
+        TubeP tp;
+        memset(&tp, 0, sizeof(tp));
+        tp.base = off;
+        tp.n = p.nx;
+        tp.order = p.order;
+        tp.limiter = p.limiter;
+        tp.gamma = p.gamma;
+        tp.R = p.R;
+        double lamy;
+        item_consts(p, &tp.CV, &tp.lam, &lamy);
+        tp.alpha = (float)p.mc_alpha;
+        tp.steps = 0;
+        tp.par = 0;
+        m->tubes.push_back(tp);
+        off += p.nx;
+    }
+    m->plane = off;
+    m->par.assign(count, 0);
+    build_chunks(m);
+    int rc = alloc_mixed(m, err, len);
+    if (rc == SHLL_OK && cudaMalloc(&m->d_chunks, sizeof(Chunk) * m->chunks.size()) != cudaSuccess) rc = SHLL_ERR_NOMEM;
+    if (rc != SHLL_OK) {
+        mixed_destroy(m);
+        return nullptr;
+    }
+    return m;
+}
+
+MixedState* mixed_create(const shll_params* p, double, double, double, cudaStream_t s, char* err, size_t len) {
+    return mixed_create_batch(p, 1, s, err, len);
+}
+
+void mixed_destroy(MixedState* m) {
+    if (!m) return;
+    if (m->d2) mixed2d_detach(m);
+    for (int b = 0; b < 2; b++) { cudaFree(m->hi[b]); cudaFree(m->lo[b]); }
+    cudaFree(m->d_tubes);
+    cudaFree(m->d_chunks);
+    cudaFree(m->d_flag);
+    delete m;
+}
+
+void mixed_set_stream(MixedState* m, cudaStream_t s) { m->stream = s; }
+
+int mixed_flags(MixedState* m) {
+    int h = 0;
+    int* f = m->d_flag;
+    if (!f) return 0;
+    cudaMemcpyAsync(&h, f, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+    cudaStreamSynchronize(m->stream);
+    return h;
+}
+
+// writes item t's conserved state (FP64, from primitive planes computed as the FP64 reference
+// does: Compute_U_from_P of base_shll.c:76-80) into buffer par[t]
+static int load_tube(MixedState* m, int t, const double* prim, char* err, size_t len) {
+    const TubeP& tp = m->tubes[t];
+    const int n = tp.n;
+    const double CV = tp.CV;
+    std::vector<double> U(3 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        double p0 = prim[i], p1 = prim[n + i], p2 = prim[2 * n + i];
+        U[i] = p0;
+        U[n + i] = p0 * p1;
+        U[2 * n + i] = p0 * (p2 * CV + 0.5 * p1 * p1);
+    }
+    m->par[t] = 0;
+    for (int k = 0; k < 3; k++) {
+        const size_t off = (size_t)k * m->plane + tp.base;
+        if (m->kahan) {
+            std::vector<float> h(n), l(n);
+            for (int i = 0; i < n; i++) {
+                h[i] = (float)U[k * n + i];
+                l[i] = (float)(U[k * n + i] - (double)h[i]);
+            }
+            if (cudaMemcpyAsync(static_cast<float*>(m->hi[0]) + off, h.data(), n * sizeof(float), cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
+                cudaMemcpyAsync(m->lo[0] + off, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
+                cudaStreamSynchronize(m->stream) != cudaSuccess) {
+                snprintf(err, len, "state upload failed");
+                return SHLL_ERR_CUDA;
+            }
+        } else {
+            if (cudaMemcpyAsync(static_cast<double*>(m->hi[0]) + off, U.data() + (size_t)k * n, n * sizeof(double),
+                                cudaMemcpyHostToDevice, m->stream) != cudaSuccess) {
+                snprintf(err, len, "state upload failed");
+                return SHLL_ERR_CUDA;
+            }
+        }
+    }
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) { snprintf(err, len, "state upload failed"); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+int mixed_load(MixedState* m, const double* prim, char* err, size_t len) {
+    cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+    if (m->dim == 2) return mixed2d_load(m, 0, prim, err, len);
+    return load_tube(m, 0, prim, err, len);
+}
+
+int mixed_load_all(MixedState* m, char* err, size_t len) {
+    cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+    for (int t = 0; t < m->nitems; t++) {
+        const shll_params& p = m->items[t];
+        std::vector<double> prim((size_t)(p.dim == 2 ? 4 : 3) * p.nx * (p.dim == 2 ? p.ny : 1));
+        shll_ic_fill(&p, 64, prim.data());
+        int rc = m->dim == 2 ? mixed2d_load(m, t, prim.data(), err, len) : load_tube(m, t, prim.data(), err, len);
+        if (rc != SHLL_OK) return rc;
+    }
+    return SHLL_OK;
+}
+
+// advances every tube by `steps[t]` steps (one launch per sweep of B steps)
+static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, size_t len) {
+    long maxsteps = 0;
+    for (int t = 0; t < m->nitems; t++) {
+        m->tubes[t].steps = (int)steps[t];
+        m->tubes[t].par = m->par[t];
+        maxsteps = std::max(maxsteps, steps[t]);
+    }
+    if (maxsteps == 0) return SHLL_OK;
+    // chunks ordered by their tube's sweep count, so launch k covers a prefix of the list
+    std::vector<Chunk> order = m->chunks;
+    std::stable_sort(order.begin(), order.end(), [&](const Chunk& x, const Chunk& y) {
+        return m->tubes[x.tube].steps > m->tubes[y.tube].steps;
+    });
+    if (cudaMemcpyAsync(m->d_tubes, m->tubes.data(), sizeof(TubeP) * m->nitems, cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
+        cudaMemcpyAsync(m->d_chunks, order.data(), sizeof(Chunk) * order.size(), cudaMemcpyHostToDevice, m->stream) != cudaSuccess) {
+        snprintf(err, len, "descriptor upload failed");
+        return SHLL_ERR_CUDA;
+    }
+    const long nsweeps = (maxsteps + m->B - 1) / m->B;
+    std::vector<int> active(nsweeps, 0);  // chunks whose tube still has sweep k
+    for (const Chunk& c : order) {
+        long sw = (m->tubes[c.tube].steps + m->B - 1) / m->B;
+        for (long k = 0; k < sw; k++) active[k]++;
+    }
+    SweepArgs A;
+    A.tubes = m->d_tubes;
+    A.chunks = m->d_chunks;
+    A.hi[0] = m->hi[0]; A.hi[1] = m->hi[1];
+    A.lo[0] = m->lo[0]; A.lo[1] = m->lo[1];
+    A.plane = m->plane;
+    A.B = m->B;
+    A.flag = m->d_flag;
+    for (long k = 0; k < nsweeps; k++) {
+        A.sweep = (int)k;
+        if (m->kahan) k_sweep1d<true><<<active[k], MT, 0, m->stream>>>(A);
+        else k_sweep1d<false><<<active[k], MT, 0, m->stream>>>(A);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { snprintf(err, len, "sweep launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    for (int t = 0; t < m->nitems; t++) {
+        long sw = (steps[t] + m->B - 1) / m->B;
+        m->par[t] = (int)((m->par[t] + sw) & 1);
+        m->cell_updates += steps[t] * (long)m->tubes[t].n;
+    }
+    return SHLL_OK;
+}
+
+int mixed_step(MixedState* m, long nsteps, char* err, size_t len) {
+    if (m->dim == 2) return mixed2d_run(m, nsteps, err, len);
+    std::vector<long> steps(m->nitems);
+    for (int t = 0; t < m->nitems; t++) steps[t] = nsteps >= 0 ? nsteps : shll_steps_for(&m->items[t]);
+    return run_tubes(m, steps, err, len);
+}
+
+long mixed_cell_updates(const MixedState* m) { return m->cell_updates; }
+
+// FP64 conserved planes of one item (rho, rho*u, E)
+static int tube_conserved(MixedState* m, int t, double* planes, char* err, size_t len) {
+    const TubeP& tp = m->tubes[t];
+    const int n = tp.n, b = m->par[t];
+    for (int k = 0; k < 3; k++) {
+        const size_t off = (size_t)k * m->plane + tp.base;
+        cudaError_t e;
+        if (m->kahan) {
+            std::vector<float> h(n), l(n);
+            e = cudaMemcpyAsync(h.data(), static_cast<float*>(m->hi[b]) + off, n * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(l.data(), m->lo[b] + off, n * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+            for (int i = 0; i < n; i++) planes[(size_t)k * n + i] = (double)h[i] + (double)l[i];
+        } else {
+            e = cudaMemcpyAsync(planes + (size_t)k * n, static_cast<double*>(m->hi[b]) + off, n * sizeof(double),
+                                cudaMemcpyDeviceToHost, m->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        }
+        if (e != cudaSuccess) { snprintf(err, len, "state download failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    }
+    return SHLL_OK;
+}
+
+int mixed_item_conserved(MixedState* m, int item, double* planes, char* err, size_t len) {
+    if (item < 0 || item >= m->nitems) { snprintf(err, len, "item %d out of range", item); return SHLL_ERR_ARG; }
+    if (m->dim == 2) return mixed2d_item_conserved(m, item, planes, err, len);
+    return tube_conserved(m, item, planes, err, len);
+}
+
+int mixed_item_primitives(MixedState* m, int item, double* rho, double* u, double* v, double* T, char* err, size_t len) {
+    if (item < 0 || item >= m->nitems) { snprintf(err, len, "item %d out of range", item); return SHLL_ERR_ARG; }
+    const shll_params& p = m->items[item];
+    const size_t n = (size_t)p.nx * (p.dim == 2 ? p.ny : 1);
+    const int nv = p.dim == 2 ? 4 : 3;
+    std::vector<double> U(nv * n);
+    int rc = mixed_item_conserved(m, item, U.data(), err, len);
+    if (rc != SHLL_OK) return rc;
+    const double CV = p.R / (p.gamma - 1.0);
+    // Compute_P_from_U in FP64 (base_shll.c:171-176 / base_shll_2d.c:312-318)
+    for (size_t c = 0; c < n; c++) {
+        double u0 = U[c];
+        double p1 = U[n + c] / u0;
+        if (nv == 3) {
+            if (rho) rho[c] = u0;
+            if (u) u[c] = p1;
+            if (T) T[c] = ((U[2 * n + c] / u0) - 0.5 * p1 * p1) / CV;
+        } else {
+            double p2 = U[2 * n + c] / u0;
+            if (rho) rho[c] = u0;
+            if (u) u[c] = p1;
+            if (v) v[c] = p2;
+            if (T) T[c] = ((U[3 * n + c] / u0) - 0.5 * (p1 * p1 + p2 * p2)) / CV;
+        }
+    }
+    return SHLL_OK;
+}
+
+int mixed_get_primitives(MixedState* m, double* rho, double* u, double* v, double* T, char* err, size_t len) {
+    return mixed_item_primitives(m, 0, rho, u, v, T, err, len);
+}
+int mixed_get_conserved(MixedState* m, double* planes, char* err, size_t len) {
+    return mixed_item_conserved(m, 0, planes, err, len);
+}
+
+int mixed_item_totals(MixedState* m, int item, double* out, char* err, size_t len) {
+    if (item < 0 || item >= m->nitems) { snprintf(err, len, "item %d out of range", item); return SHLL_ERR_ARG; }
+    if (m->dim == 2) return mixed2d_totals(m, item, out, err, len);
+    const TubeP& tp = m->tubes[item];
+    const int b = m->par[item];
+    double tmp[3];
+    for (int k = 0; k < 3; k++) {
+        const size_t off = (size_t)k * m->plane + tp.base;
+        cudaError_t e = m->kahan
+            ? device_pair_sums(static_cast<float*>(m->hi[b]) + off, m->lo[b] + off, 1, tp.n, &tmp[k], m->stream)
+            : device_plane_sums(static_cast<double*>(m->hi[b]) + off, 64, 1, tp.n, &tmp[k], m->stream);
+        if (e != cudaSuccess) { snprintf(err, len, "totals failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    }
+    for (int k = 0; k < 3; k++) out[k] = tmp[k];
+    return SHLL_OK;
+}
+
+int mixed_totals(MixedState* m, double* out, char* err, size_t len) { return mixed_item_totals(m, 0, out, err, len); }
+
+// accessors used by mixed2d.cu
+cudaStream_t mixed_stream(MixedState* m) { return m->stream; }
+int* mixed_flag_ptr(MixedState* m) { return m->d_flag; }
+const shll_params* mixed_items(MixedState* m, int* count) { *count = m->nitems; return m->items.data(); }
+void** mixed_d2_slot(MixedState* m) { return &m->d2; }
+int mixed_fold(MixedState* m) { return m->B; }
+bool mixed_is_kahan(MixedState* m) { return m->kahan; }
+void mixed_add_updates(MixedState* m, long u) { m->cell_updates += u; }

@@ -1,0 +1,282 @@
+"""ctypes binding of libshll_gb300.so (the C-ABI declared in include/shll.h).
+
+This is the host-side mirror of the reference's solver stages (archembaud/shll-sve-cfd,
+base-c/base_shll.c:28-225): a Context owns one problem on the GPU and exposes
+init_state (Allocate_and_Init_Memory + Compute_U_from_P + Compute_P_from_U), the four stages,
+run (the time loop), and the results.  There is no CPU fallback: loading fails loudly if the
+library has not been built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libshll_gb300.so")
+
+OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NUMERIC, ERR_TIMEOUT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7
+PREC_F64, PREC_F64_EXACT, PREC_F32_EXACT, PREC_MIXED_F64, PREC_MIXED_KAHAN = 0, 1, 2, 3, 4
+IC_SOD, IC_REF_BOX2D, IC_CIRCLE2D, IC_FOUR_SHOCK2D, IC_USER, IC_QUADRANTS2D = 0, 1, 2, 3, 4, 5
+PRECISIONS = {"f64": PREC_F64, "f64_exact": PREC_F64_EXACT, "f32_exact": PREC_F32_EXACT,
+              "mixed_f64": PREC_MIXED_F64, "mixed_kahan": PREC_MIXED_KAHAN}
+
+
+class Ic(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("x_d", ctypes.c_double),
+                ("rho_l", ctypes.c_double), ("u_l", ctypes.c_double), ("T_l", ctypes.c_double),
+                ("rho_r", ctypes.c_double), ("u_r", ctypes.c_double), ("T_r", ctypes.c_double),
+                ("cx", ctypes.c_double), ("cy", ctypes.c_double), ("radius", ctypes.c_double)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("order", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("gamma", ctypes.c_double), ("R", ctypes.c_double), ("cfl", ctypes.c_double),
+                ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("t_end", ctypes.c_double),
+                ("n_steps", ctypes.c_long), ("precision", ctypes.c_int), ("limiter", ctypes.c_int),
+                ("mc_alpha", ctypes.c_double), ("fold_steps", ctypes.c_int), ("clock_f32", ctypes.c_int),
+                ("ic", Ic)]
+
+
+class ShllError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+EXPORTS = [
+    "shll_params_default", "shll_steps_for", "shll_create", "shll_destroy", "shll_last_error",
+    "shll_status_string", "shll_set_stream", "shll_init_state", "shll_set_primitives",
+    "shll_compute_U_from_P", "shll_compute_P_from_U", "shll_compute_F_from_P", "shll_update_U_from_F",
+    "shll_step", "shll_run", "shll_steps_taken", "shll_get_primitives", "shll_get_conserved",
+    "shll_get_fluxes", "shll_totals", "shll_save_results", "shll_batch_create", "shll_batch_run",
+    "shll_batch_get_primitives", "shll_batch_totals", "shll_batch_cell_updates", "shll_batch_last_error",
+    "shll_batch_destroy", "shll_ref_configure", "shll_ref_context", "Allocate_and_Init_Memory",
+    "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P", "Update_U_from_F", "Save_Results",
+    "Free_Memory", "shll_ref_dt",
+]
+
+
+def lib():
+    """Loads the library (built by build.py / __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libshll_gb300.so not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        vp = ctypes.c_void_p
+        P = ctypes.POINTER(Params)
+        L.shll_params_default.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.shll_params_default.restype = None
+        L.shll_steps_for.argtypes = [P]
+        L.shll_steps_for.restype = ctypes.c_long
+        L.shll_create.argtypes = [P, ctypes.POINTER(vp)]
+        L.shll_destroy.argtypes = [vp]
+        L.shll_destroy.restype = None
+        L.shll_last_error.argtypes = [vp]
+        L.shll_last_error.restype = ctypes.c_char_p
+        L.shll_status_string.argtypes = [ctypes.c_int]
+        L.shll_status_string.restype = ctypes.c_char_p
+        L.shll_set_stream.argtypes = [vp, vp]
+        for f in ("shll_init_state", "shll_compute_U_from_P", "shll_compute_P_from_U", "shll_compute_F_from_P",
+                  "shll_update_U_from_F"):
+            getattr(L, f).argtypes = [vp]
+        L.shll_set_primitives.argtypes = [vp, dp, dp, dp, dp]
+        L.shll_step.argtypes = [vp, ctypes.c_long]
+        L.shll_run.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+        L.shll_steps_taken.argtypes = [vp]
+        L.shll_steps_taken.restype = ctypes.c_long
+        L.shll_get_primitives.argtypes = [vp, dp, dp, dp, dp]
+        L.shll_get_conserved.argtypes = [vp, dp]
+        L.shll_get_fluxes.argtypes = [vp, dp, dp, dp, dp]
+        L.shll_totals.argtypes = [vp, dp]
+        L.shll_save_results.argtypes = [vp, ctypes.c_char_p]
+        L.shll_batch_create.argtypes = [P, ctypes.c_int, ctypes.POINTER(vp)]
+        L.shll_batch_run.argtypes = [vp]
+        L.shll_batch_get_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
+        L.shll_batch_totals.argtypes = [vp, ctypes.c_int, dp]
+        L.shll_batch_cell_updates.argtypes = [vp]
+        L.shll_batch_cell_updates.restype = ctypes.c_long
+        L.shll_batch_last_error.argtypes = [vp]
+        L.shll_batch_last_error.restype = ctypes.c_char_p
+        L.shll_batch_destroy.argtypes = [vp]
+        L.shll_batch_destroy.restype = None
+        L.shll_ref_configure.argtypes = [P]
+        L.shll_ref_context.restype = vp
+        L.shll_ref_dt.restype = ctypes.c_double
+        for f in ("Allocate_and_Init_Memory", "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P",
+                  "Update_U_from_F", "Save_Results", "Free_Memory"):
+            getattr(L, f).restype = None
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def params(dim=1, order=1, nx=256, ny=None, precision="f64", **kw):
+    """Reference defaults for (dim, order) with overrides; ic_* keys set the initial data."""
+    p = Params()
+    lib().shll_params_default(ctypes.byref(p), dim, order)
+    p.nx = nx
+    p.ny = (ny if ny is not None else nx) if dim == 2 else 1
+    p.precision = PRECISIONS[precision] if isinstance(precision, str) else precision
+    for k, v in kw.items():
+        if k.startswith("ic_"):
+            setattr(p.ic, k[3:], v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def steps_for(p):
+    return lib().shll_steps_for(ctypes.byref(p))
+
+
+class Context:
+    """One problem on the GPU (a shll_ctx)."""
+
+    def __init__(self, p):
+        self.p = p
+        self.h = ctypes.c_void_p()
+        rc = lib().shll_create(ctypes.byref(p), ctypes.byref(self.h))
+        if rc != OK:
+            raise ShllError(rc, "shll_create failed: " + lib().shll_status_string(rc).decode())
+        self.n = p.nx * (p.ny if p.dim == 2 else 1)
+        self.nv = 4 if p.dim == 2 else 3
+
+    def _ck(self, rc, what):
+        if rc != OK:
+            raise ShllError(rc, f"{what}: {lib().shll_last_error(self.h).decode()}")
+        return rc
+
+    def close(self):
+        if self.h:
+            lib().shll_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_state(self):
+        return self._ck(lib().shll_init_state(self.h), "init_state")
+
+    def set_primitives(self, rho, u, T, v=None):
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (rho, u, T)]
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        return self._ck(lib().shll_set_primitives(self.h, _dp(arrs[0]), _dp(arrs[1]), _dp(vv), _dp(arrs[2])),
+                        "set_primitives")
+
+    def compute_U_from_P(self):
+        return self._ck(lib().shll_compute_U_from_P(self.h), "Compute_U_from_P")
+
+    def compute_P_from_U(self):
+        return self._ck(lib().shll_compute_P_from_U(self.h), "Compute_P_from_U")
+
+    def compute_F_from_P(self):
+        return self._ck(lib().shll_compute_F_from_P(self.h), "Compute_F_from_P")
+
+    def update_U_from_F(self):
+        return self._ck(lib().shll_update_U_from_F(self.h), "Update_U_from_F")
+
+    def step(self, n):
+        return self._ck(lib().shll_step(self.h, n), "step")
+
+    def run(self):
+        s = ctypes.c_long()
+        self._ck(lib().shll_run(self.h, ctypes.byref(s)), "run")
+        return s.value
+
+    @property
+    def steps_taken(self):
+        return lib().shll_steps_taken(self.h)
+
+    def primitives(self):
+        """(nv, n) array: rho, u, [v,] T."""
+        out = np.zeros((self.nv, self.n))
+        if self.nv == 3:
+            self._ck(lib().shll_get_primitives(self.h, _dp(out[0]), _dp(out[1]), None, _dp(out[2])), "primitives")
+        else:
+            self._ck(lib().shll_get_primitives(self.h, _dp(out[0]), _dp(out[1]), _dp(out[2]), _dp(out[3])),
+                     "primitives")
+        return out
+
+    def conserved(self):
+        out = np.zeros((self.nv, self.n))
+        self._ck(lib().shll_get_conserved(self.h, _dp(out)), "conserved")
+        return out
+
+    def fluxes(self):
+        fp, fm = np.zeros((self.nv, self.n)), np.zeros((self.nv, self.n))
+        if self.nv == 4:
+            hp, hm = np.zeros((self.nv, self.n)), np.zeros((self.nv, self.n))
+            self._ck(lib().shll_get_fluxes(self.h, _dp(fp), _dp(fm), _dp(hp), _dp(hm)), "fluxes")
+            return fp, fm, hp, hm
+        self._ck(lib().shll_get_fluxes(self.h, _dp(fp), _dp(fm), None, None), "fluxes")
+        return fp, fm
+
+    def totals(self):
+        out = np.zeros(self.nv)
+        self._ck(lib().shll_totals(self.h, _dp(out)), "totals")
+        return out
+
+    def save_results(self, path):
+        return self._ck(lib().shll_save_results(self.h, path.encode()), "save_results")
+
+
+class Batch:
+    """Many independent tubes or domains advanced together (a shll_batch)."""
+
+    def __init__(self, items):
+        arr = (Params * len(items))(*items)
+        self.items = items
+        self.h = ctypes.c_void_p()
+        rc = lib().shll_batch_create(arr, len(items), ctypes.byref(self.h))
+        if rc != OK:
+            raise ShllError(rc, "shll_batch_create failed: " + lib().shll_status_string(rc).decode())
+
+    def _ck(self, rc, what):
+        if rc != OK:
+            raise ShllError(rc, f"{what}: {lib().shll_batch_last_error(self.h).decode()}")
+
+    def run(self):
+        self._ck(lib().shll_batch_run(self.h), "batch_run")
+
+    def primitives(self, i):
+        p = self.items[i]
+        n = p.nx * (p.ny if p.dim == 2 else 1)
+        nv = 4 if p.dim == 2 else 3
+        out = np.zeros((nv, n))
+        if nv == 3:
+            self._ck(lib().shll_batch_get_primitives(self.h, i, _dp(out[0]), _dp(out[1]), None, _dp(out[2])), "prims")
+        else:
+            self._ck(lib().shll_batch_get_primitives(self.h, i, _dp(out[0]), _dp(out[1]), _dp(out[2]), _dp(out[3])),
+                     "prims")
+        return out
+
+    def totals(self, i):
+        nv = 4 if self.items[i].dim == 2 else 3
+        out = np.zeros(nv)
+        self._ck(lib().shll_batch_totals(self.h, i, _dp(out)), "totals")
+        return out
+
+    @property
+    def cell_updates(self):
+        return lib().shll_batch_cell_updates(self.h)
+
+    def close(self):
+        if self.h:
+            lib().shll_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

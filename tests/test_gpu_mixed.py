@@ -1,0 +1,91 @@
+"""GPU tests of the mixed-precision engine (FP32 perturbation-form fluxes, compensated FP32
+accumulation, FP64 or FP32-pair state) against the FP64 oracle.
+
+Tolerances: L1(rho, u, T) <= 1e-6 against the FP64 oracle for first-order tubes at any size
+tested and for second-order tubes up to 1024 cells; mass (and energy, with reflective walls)
+conserved to <= 1e-12 relative.  Second-order runs on long tubes amplify any rounding difference
+(even FP64 with and without fused multiply-add differ by L1(rho) ~ 8e-7 at 65536 cells), so
+larger second-order cases are checked against the exact Riemann solution instead."""
+import numpy as np
+import pytest
+
+from helpers import l1
+
+pytestmark = pytest.mark.gpu
+
+
+def run_mixed(shll, p):
+    ctx = shll.Context(p)
+    ctx.init_state()
+    t0 = ctx.totals()
+    steps = ctx.run()
+    out = ctx.primitives()
+    t1 = ctx.totals()
+    ctx.close()
+    return steps, out, t0, t1
+
+
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+@pytest.mark.parametrize("order,n", [(1, 2), (1, 37), (1, 256), (1, 1024), (1, 4096), (2, 64), (2, 512), (2, 1024)])
+def test_mixed_1d_vs_fp64_oracle(shll, oracle, prec, order, n):
+    steps, ref, _ = oracle.run(oracle.make_cfg(order=order, nx=n), oracle.ic_sod(n))
+    s, out, t0, t1 = run_mixed(shll, shll.params(1, order, nx=n, precision=prec))
+    assert s == steps
+    err = l1(out, ref)
+    assert np.all(err <= 1e-6), err
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+    if order == 1:
+        assert abs(t1[2] - t0[2]) / t0[2] <= 1e-12
+
+
+@pytest.mark.parametrize("fold", [1, 4, 32])
+def test_fold_interval(shll, oracle, fold):
+    n = 2000  # several chunks: exercises the frame boundaries
+    steps, ref, _ = oracle.run(oracle.make_cfg(nx=n), oracle.ic_sod(n))
+    s, out, t0, t1 = run_mixed(shll, shll.params(1, 1, nx=n, precision="mixed_f64", fold_steps=fold))
+    assert s == steps
+    assert np.all(l1(out, ref) <= 1e-6)
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-13
+
+
+def test_partial_steps_then_run(shll, oracle):
+    n = 1500
+    _, ref, _ = oracle.run(oracle.make_cfg(nx=n), oracle.ic_sod(n))
+    ctx = shll.Context(shll.params(1, 1, nx=n, precision="mixed_f64"))
+    ctx.init_state()
+    ctx.step(7)
+    ctx.step(100)
+    ctx.run()
+    assert np.all(l1(ctx.primitives(), ref) <= 1e-6)
+
+
+def test_second_order_large_tube_vs_exact_riemann(shll, oracle):
+    n = 8192
+    s, out, t0, t1 = run_mixed(shll, shll.params(1, 2, nx=n, precision="mixed_f64"))
+    ex = oracle.riemann_exact(n, s * (0.125 / n))
+    assert np.mean(np.abs(out[0] - ex[0])) < 0.003
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+
+
+def test_batch_matches_single_contexts_and_oracle(shll, oracle):
+    rng = np.random.default_rng(3)
+    items, refs = [], []
+    for i in range(12):
+        n = int(rng.integers(40, 1800))
+        order = 1 + (i % 2)
+        rl, tl, xd = float(rng.uniform(2, 20)), float(rng.uniform(0.5, 2)), float(rng.uniform(0.3, 0.7))
+        p = shll.params(1, order, nx=n, precision="mixed_f64", ic_x_d=xd, ic_rho_l=rl, ic_T_l=tl)
+        items.append(p)
+        prim = oracle.ic_sod(n, x_d=xd, rhoL=rl, TL=tl)
+        refs.append(oracle.run(oracle.make_cfg(order=order, nx=n), prim)[1])
+    b = shll.Batch(items)
+    b.run()
+    for i, p in enumerate(items):
+        out = b.primitives(i)
+        tol = 1e-6 if (p.order == 1 or p.nx <= 1024) else 1e-4
+        assert np.all(l1(out, refs[i]) <= tol), (i, p.nx, p.order, l1(out, refs[i]))
+        single = shll.Context(p)
+        single.init_state()
+        single.run()
+        assert np.array_equal(single.primitives(), out)
+    assert b.cell_updates == sum(p.nx * shll.steps_for(p) for p in items)
