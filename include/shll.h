@@ -138,6 +138,15 @@ int shll_step(shll_ctx* ctx, long n);
 int shll_run(shll_ctx* ctx, long* steps_taken);
 long shll_steps_taken(const shll_ctx* ctx);
 
+/* ---- checkpoint / resume on the device ----
+ * The reference keeps no checkpoint (results.dat is its only output).  shll_checkpoint copies
+ * the state and the step counter into device memory owned by the context; shll_restore puts
+ * them back, so a run can be repeated from the same state or split at any step. */
+int shll_checkpoint(shll_ctx* ctx);
+int shll_restore(shll_ctx* ctx);
+/* Number of CUDA kernels this library has launched in the process so far. */
+long shll_kernel_launches(void);
+
 /* ---- results (host copies) ---- */
 int shll_get_primitives(shll_ctx* ctx, double* rho, double* u, double* v, double* T);
 /* conserved planes rho, rho*u, [rho*v,] E, each nx*ny doubles, written contiguously */

@@ -2,6 +2,7 @@
 // results, and the reference's own entry-point names on a default context.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -29,6 +30,11 @@ struct shll_ctx {
     void* P = nullptr;
     void* F[4] = {nullptr, nullptr, nullptr, nullptr};  // fp, fm, hp, hm (staged; lazily allocated)
     bool fluxes_valid = false;
+    // device checkpoint of the plain state
+    void* ckU = nullptr;
+    void* ckP = nullptr;
+    long ck_steps = -1;
+    int ck_cur = 0;
     // mixed state
     MixedState* mixed = nullptr;
     int* d_flag = nullptr;
@@ -280,7 +286,7 @@ extern "C" int shll_create(const shll_params* p, shll_ctx** out) {
 extern "C" void shll_destroy(shll_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->U[0]); cudaFree(c->U[1]); cudaFree(c->P);
+    cudaFree(c->U[0]); cudaFree(c->U[1]); cudaFree(c->P); cudaFree(c->ckU); cudaFree(c->ckP);
     for (int k = 0; k < 4; k++) cudaFree(c->F[k]);
     cudaFree(c->d_flag);
     if (c->mixed) mixed_destroy(c->mixed);
@@ -450,6 +456,47 @@ extern "C" int shll_run(shll_ctx* c, long* steps_taken) {
 }
 
 extern "C" long shll_steps_taken(const shll_ctx* c) { return c ? c->steps_taken : -1; }
+
+static std::atomic<long> g_launches{0};
+void shll_count_launches(long n) { g_launches += n; }
+extern "C" long shll_kernel_launches(void) { return g_launches.load(); }
+
+extern "C" int shll_checkpoint(shll_ctx* c) {
+    if (!c) return SHLL_ERR_ARG;
+    if (!c->initialized) { set_err(c, "state not initialised"); return SHLL_ERR_STATE; }
+    if (!c->plain) {
+        int rc = mixed_checkpoint(c->mixed, false, c->err, sizeof(c->err));
+        if (rc == SHLL_OK) c->ck_steps = c->steps_taken;
+        return rc;
+    }
+    const size_t rb = c->real_bits / 8, n = (size_t)c->n;
+    if (!c->ckU) {
+        CUDA_TRY(c, cudaMalloc(&c->ckU, c->nv * n * rb));
+        CUDA_TRY(c, cudaMalloc(&c->ckP, (c->nv + 1) * n * rb));
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c->ckU, c->U[c->cur], c->nv * n * rb, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->ckP, c->P, (c->nv + 1) * n * rb, cudaMemcpyDeviceToDevice, c->stream));
+    c->ck_steps = c->steps_taken;
+    c->ck_cur = c->cur;
+    return SHLL_OK;
+}
+
+extern "C" int shll_restore(shll_ctx* c) {
+    if (!c) return SHLL_ERR_ARG;
+    if (c->ck_steps < 0) { set_err(c, "no checkpoint taken"); return SHLL_ERR_STATE; }
+    if (!c->plain) {
+        int rc = mixed_checkpoint(c->mixed, true, c->err, sizeof(c->err));
+        if (rc == SHLL_OK) c->steps_taken = c->ck_steps;
+        return rc;
+    }
+    const size_t rb = c->real_bits / 8, n = (size_t)c->n;
+    c->cur = c->ck_cur;
+    CUDA_TRY(c, cudaMemcpyAsync(c->U[c->cur], c->ckU, c->nv * n * rb, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->P, c->ckP, (c->nv + 1) * n * rb, cudaMemcpyDeviceToDevice, c->stream));
+    c->steps_taken = c->ck_steps;
+    c->fluxes_valid = false;
+    return SHLL_OK;
+}
 
 template <typename REAL>
 static void widen(const std::vector<unsigned char>& src, size_t off, size_t n, double* dst) {

@@ -30,6 +30,7 @@ int mixed_item_primitives(MixedState* m, int item, double* rho, double* u, doubl
 int mixed_item_totals(MixedState* m, int item, double* out, char* err, size_t errlen);
 int mixed_item_conserved(MixedState* m, int item, double* planes, char* err, size_t errlen);
 long mixed_cell_updates(const MixedState* m);
+int mixed_checkpoint(MixedState* m, bool restore, char* err, size_t errlen);
 int mixed_flags(MixedState* m);
 
 // FP64 plane sums (reduce.cu)

@@ -364,31 +364,34 @@ struct MixedState {
     std::vector<Chunk> chunks;         // sorted by the steps of their tube (descending)
     int* d_flag = nullptr;
     long cell_updates = 0;
+    // device checkpoint (shll_checkpoint)
+    void* ck_hi[2] = {nullptr, nullptr};
+    float* ck_lo[2] = {nullptr, nullptr};
+    std::vector<int> ck_par;
+    long ck_updates = 0;
     // 2D engine (mixed2d.cu)
     void* d2 = nullptr;
 };
 
 static int chunk_owned(int order, int B) { return MW - 2 * order * B; }
 
+// Chunks of every tube.  A tube has at least two chunks; the first chunk's frame is anchored
+// at the left wall cell and the last chunk's at the right wall cell, so that a wall region
+// still equal to its wall cell has exactly zero split-flux deviations (as in the reference, a
+// gas at rest next to a wall stays exactly at rest); interior chunks anchor at their centre.
 static void build_chunks(MixedState* m) {
     m->chunks.clear();
     for (int t = 0; t < m->nitems; t++) {
         const TubeP& tp = m->tubes[t];
         const int n = tp.n;
-        if (n <= MW) {
-            m->chunks.push_back({t, 0, n, -1, n / 2, -1});
-            continue;
-        }
         const int S = chunk_owned(tp.order, m->B);
-        const int k = (n + S - 1) / S;
-        std::vector<int> edges(k + 1);
+        int k = n <= MW ? 2 : (n + S - 1) / S;
+        if (k > n) k = n;
+        std::vector<int> edges(k + 1), anc(k);
         for (int c = 0; c <= k; c++) edges[c] = (int)((long)n * c / k);
-        for (int c = 0; c < k; c++) {
-            int a = edges[c], b = edges[c + 1];
-            int ancL = c > 0 ? (edges[c - 1] + a) / 2 : -1;
-            int ancR = c + 1 < k ? (b + edges[c + 2]) / 2 : -1;
-            m->chunks.push_back({t, a, b, ancL, (a + b) / 2, ancR});
-        }
+        for (int c = 0; c < k; c++) anc[c] = c == 0 ? 0 : (c == k - 1 ? n - 1 : (edges[c] + edges[c + 1]) / 2);
+        for (int c = 0; c < k; c++)
+            m->chunks.push_back({t, edges[c], edges[c + 1], c > 0 ? anc[c - 1] : -1, anc[c], c + 1 < k ? anc[c + 1] : -1});
     }
 }
 
@@ -496,7 +499,9 @@ MixedState* mixed_create(const shll_params* p, double, double, double, cudaStrea
 void mixed_destroy(MixedState* m) {
     if (!m) return;
     if (m->d2) mixed2d_detach(m);
-    for (int b = 0; b < 2; b++) { cudaFree(m->hi[b]); cudaFree(m->lo[b]); }
+    for (int b = 0; b < 2; b++) {
+        cudaFree(m->hi[b]); cudaFree(m->lo[b]); cudaFree(m->ck_hi[b]); cudaFree(m->ck_lo[b]);
+    }
     cudaFree(m->d_tubes);
     cudaFree(m->d_chunks);
     cudaFree(m->d_flag);
@@ -605,6 +610,7 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     A.plane = m->plane;
     A.B = m->B;
     A.flag = m->d_flag;
+    shll_count_launches(nsweeps);
     for (long k = 0; k < nsweeps; k++) {
         A.sweep = (int)k;
         if (m->kahan) k_sweep1d<true><<<active[k], MT, 0, m->stream>>>(A);
@@ -720,3 +726,28 @@ void** mixed_d2_slot(MixedState* m) { return &m->d2; }
 int mixed_fold(MixedState* m) { return m->B; }
 bool mixed_is_kahan(MixedState* m) { return m->kahan; }
 void mixed_add_updates(MixedState* m, long u) { m->cell_updates += u; }
+
+// copies both state buffers (the buffer a tube lives in differs per tube) and the parities
+int mixed_checkpoint(MixedState* m, bool restore, char* err, size_t len) {
+    if (m->dim == 2) { snprintf(err, len, "checkpoint of 2D mixed state not supported"); return SHLL_ERR_UNSUPPORTED; }
+    const size_t vb = (size_t)m->plane * 3 * (m->kahan ? sizeof(float) : sizeof(double));
+    const size_t lb = (size_t)m->plane * 3 * sizeof(float);
+    if (restore && !m->ck_hi[0]) { snprintf(err, len, "no checkpoint taken"); return SHLL_ERR_STATE; }
+    for (int b = 0; b < 2; b++) {
+        if (!restore && !m->ck_hi[b]) {
+            if (cudaMalloc(&m->ck_hi[b], vb) != cudaSuccess || (m->kahan && cudaMalloc(&m->ck_lo[b], lb) != cudaSuccess)) {
+                snprintf(err, len, "checkpoint allocation failed");
+                return SHLL_ERR_NOMEM;
+            }
+        }
+        cudaError_t e = restore ? cudaMemcpyAsync(m->hi[b], m->ck_hi[b], vb, cudaMemcpyDeviceToDevice, m->stream)
+                                : cudaMemcpyAsync(m->ck_hi[b], m->hi[b], vb, cudaMemcpyDeviceToDevice, m->stream);
+        if (e == cudaSuccess && m->kahan)
+            e = restore ? cudaMemcpyAsync(m->lo[b], m->ck_lo[b], lb, cudaMemcpyDeviceToDevice, m->stream)
+                        : cudaMemcpyAsync(m->ck_lo[b], m->lo[b], lb, cudaMemcpyDeviceToDevice, m->stream);
+        if (e != cudaSuccess) { snprintf(err, len, "checkpoint copy failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    }
+    if (restore) { m->par = m->ck_par; m->cell_updates = m->ck_updates; }
+    else { m->ck_par = m->par; m->ck_updates = m->cell_updates; }
+    return SHLL_OK;
+}

@@ -40,7 +40,7 @@ __device__ __forceinline__ void ff_add(float ah, float al, float bh, float bl, f
     float e = __fadd_rn(__fadd_rn(ah, -__fadd_rn(s, -bp)), __fadd_rn(bh, -bp));
     e = __fadd_rn(e, __fadd_rn(al, bl));
     oh = __fadd_rn(s, e);
-    ol = __fadd_rn(e, -__fadd_rn(oh, s));
+    ol = __fadd_rn(e, -__fadd_rn(oh, -s));
 }
 __device__ __forceinline__ void ff_sub(float ah, float al, float bh, float bl, float& oh, float& ol) {
     ff_add(ah, al, -bh, -bl, oh, ol);

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "mixed.h"
+#include "shll_internal.h"
 
 namespace {
 constexpr int RB = 256;     // threads per block
@@ -46,6 +47,7 @@ static cudaError_t sums_t(const T* hi, const T* lo, int nv, long n, double* out,
     double* d = nullptr;
     cudaError_t e = cudaMallocAsync(&d, sizeof(double) * nv * RGRID, s);
     if (e != cudaSuccess) return e;
+    shll_count_launches(1);
     k_plane_sums<T><<<RGRID, RB, 0, s>>>(hi, lo, nv, n, d);
     std::vector<double> h((size_t)nv * RGRID);
     e = cudaGetLastError();

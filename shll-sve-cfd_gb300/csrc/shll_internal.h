@@ -8,6 +8,9 @@
 #define SHLL_FLAG_TIMEOUT 2       // a bounded device-side wait gave up
 #define SHLL_FLAG_BADARG 4        // a kernel rejected its launch arguments
 
+// kernel launches issued by the library (shll_kernel_launches)
+void shll_count_launches(long n);
+
 enum { STAGE_U_FROM_P = 0, STAGE_P_FROM_U = 1, STAGE_F_FROM_P = 2, STAGE_UPDATE = 3 };
 
 // Arguments of the plain (reference-arithmetic) kernels.  The constants are the reference's

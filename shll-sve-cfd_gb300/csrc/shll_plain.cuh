@@ -423,6 +423,7 @@ __global__ void k_update_staged(REAL* __restrict__ U, const REAL* __restrict__ f
 // ---------------- host launchers ----------------
 template <typename REAL>
 static cudaError_t step_t(const PlainArgs& a) {
+    shll_count_launches(1);
     Gas<REAL> g = make_gas<REAL>(a);
     const REAL* Uin = static_cast<const REAL*>(a.Uin);
     REAL* Uout = static_cast<REAL*>(a.Uout);
@@ -447,6 +448,7 @@ static cudaError_t step_t(const PlainArgs& a) {
 
 template <typename REAL>
 static cudaError_t stage_t(const PlainArgs& a, int which) {
+    shll_count_launches(1);
     Gas<REAL> g = make_gas<REAL>(a);
     const int n = a.nx * (a.dim == 2 ? a.ny : 1);
     const int threads = 256;

@@ -54,7 +54,7 @@ EXPORTS = [
     "shll_batch_get_primitives", "shll_batch_totals", "shll_batch_cell_updates", "shll_batch_last_error",
     "shll_batch_destroy", "shll_ref_configure", "shll_ref_context", "Allocate_and_Init_Memory",
     "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P", "Update_U_from_F", "Save_Results",
-    "Free_Memory", "shll_ref_dt",
+    "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
 ]
 
 
@@ -106,6 +106,9 @@ def lib():
         L.shll_ref_configure.argtypes = [P]
         L.shll_ref_context.restype = vp
         L.shll_ref_dt.restype = ctypes.c_double
+        L.shll_checkpoint.argtypes = [vp]
+        L.shll_restore.argtypes = [vp]
+        L.shll_kernel_launches.restype = ctypes.c_long
         for f in ("Allocate_and_Init_Memory", "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P",
                   "Update_U_from_F", "Save_Results", "Free_Memory"):
             getattr(L, f).restype = None
@@ -134,6 +137,10 @@ def params(dim=1, order=1, nx=256, ny=None, precision="f64", **kw):
 
 def steps_for(p):
     return lib().shll_steps_for(ctypes.byref(p))
+
+
+def kernel_launches():
+    return lib().shll_kernel_launches()
 
 
 class Context:
@@ -225,6 +232,15 @@ class Context:
         out = np.zeros(self.nv)
         self._ck(lib().shll_totals(self.h, _dp(out)), "totals")
         return out
+
+    def checkpoint(self):
+        return self._ck(lib().shll_checkpoint(self.h), "checkpoint")
+
+    def restore(self):
+        return self._ck(lib().shll_restore(self.h), "restore")
+
+    def set_stream(self, stream_ptr):
+        return self._ck(lib().shll_set_stream(self.h, stream_ptr), "set_stream")
 
     def save_results(self, path):
         return self._ck(lib().shll_save_results(self.h, path.encode()), "save_results")

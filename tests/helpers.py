@@ -9,12 +9,17 @@ def max_rel(a, b, floor=1e-300):
 
 
 def max_rel_scaled(a, b):
-    """max per-cell relative difference, with each field's difference taken relative to
-    max(|b_cell|, 1e-12 * max|b|) so that cells where a velocity is ~0 do not divide by ~0."""
+    """Max per-cell relative difference of primitive planes (rho, u, [v,] T): density and
+    temperature (positive everywhere) relative to each cell's value; velocities, which pass
+    through zero, relative to the field's largest magnitude."""
     a, b = np.asarray(a), np.asarray(b)
+    nv = a.shape[0]
     out = 0.0
-    for k in range(a.shape[0]):
-        scale = np.maximum(np.abs(b[k]), 1e-12 * np.max(np.abs(b[k])) + 1e-300)
+    for k in range(nv):
+        if k in (0, nv - 1):
+            scale = np.abs(b[k])
+        else:
+            scale = np.full_like(b[k], max(np.max(np.abs(b[k])), 1e-300))
         out = max(out, float(np.max(np.abs(a[k] - b[k]) / scale)))
     return out
 
