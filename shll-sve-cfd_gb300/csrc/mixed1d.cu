@@ -3,28 +3,31 @@
 //
 // Scheme (the arithmetic of base-c/base_shll.c:87-159 and of the x sweep of
 // base-c/2nd_order_base_shll.c:203-459, re-associated as interface fluxes):
-//   * Cells are grouped in chunks (one CTA each).  Every chunk has a frame: the FP64 state U* of
-//     its centre cell at the start of the sweep and the split-flux coefficients derived from it.
-//   * A cell's split fluxes are evaluated in FP32 as deviations from the frame's
-//     (d fp = fp(U) - fp(U*), d fm likewise), using only deviations as FP32 operands, so their
-//     rounding error scales with |U - U*| instead of |U|.
-//   * The flux through interface j+1/2 is Fref(frame of cell j) + Delta_{j+1/2}; Delta uses
-//     cells j-1..j+2 expressed in that frame.  Both neighbouring cells add the same value (with
-//     opposite signs), so the scheme is conservative to rounding of the state; a cell whose left
-//     neighbour lies in another frame also adds lam*(Fref_left - Fref_own) (FP64, as an FP32 pair).
-//     Chunks recompute their neighbours' halo cells in the NEIGHBOUR's frame, so every chunk
-//     evaluates every interface bit for bit like its owner (this file is compiled with
-//     -fmad=false; fused operations are explicit).
-//   * Per step, lam*Delta terms are added to an FP32 value+compensation pair per cell (TwoSum).
-//     At the end of a sweep (fold_steps steps) the pair is added to the stored state: in FP64
+//   * Cells are grouped in chunks (one CTA each).  A chunk is computed over a window of its own
+//     cells plus a halo of order*steps cells on each side (temporal blocking), so one launch
+//     advances every chunk of every tube by a whole sweep of fold_steps steps, with no inter-CTA
+//     waits.
+//   * Every chunk has one frame: the FP64 state U* of an anchor cell at the start of the sweep
+//     (the wall cell for the first and last chunk of a tube, else the centre cell) and the
+//     split-flux coefficients derived from it.  Each window cell's split fluxes are evaluated in
+//     FP32 as deviations from the frame (d fp = fp(U) - fp(U*), d fm likewise), with only
+//     deviations as FP32 operands, so their rounding error scales with |U - U*| instead of |U|.
+//   * The flux through interface j+1/2 is Fref + Delta_{j+1/2} (Fref = the anchor's physical
+//     flux, which cancels inside a chunk); both neighbouring cells add the same FP32 value
+//     lam*Delta with opposite signs (TwoSum into an FP32 value+compensation pair per cell).
+//   * Neighbouring chunks evaluate their shared boundary interface in different frames, so the
+//     two values differ by rounding.  Each chunk records the flux it applied at both of its
+//     boundaries over the sweep; at the next load the right chunk's first cell receives
+//     lam*sum(F_left chunk - F_right chunk), which makes the left chunk's value the one that
+//     counts: mass, momentum and energy are conserved to the rounding of the FP64 state.
+//   * At the end of a sweep the pair is added to the stored state: in FP64
 //     (SHLL_PREC_MIXED_F64) or in FP32-pair arithmetic (SHLL_PREC_MIXED_KAHAN).
-//   * A chunk is computed with a halo of order*steps cells on each side (temporal blocking), so
-//     one launch advances every chunk of every tube by a whole sweep with no inter-CTA waits.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -34,9 +37,9 @@
 
 namespace {
 
-constexpr int MT = 128;       // threads per CTA
-constexpr int MC = 4;         // cells per thread
-constexpr int MW = MT * MC;   // window capacity (cells)
+constexpr int MW = 512;       // window capacity (cells) of one CTA
+constexpr int MC = 1;         // cells per thread
+constexpr int MT = MW / MC;   // threads per CTA
 
 struct TubeP {
     long base;        // offset of cell 0 in the planes
@@ -49,8 +52,9 @@ struct TubeP {
 
 struct Chunk {
     int tube;
-    int a, b;                // owned cells [a, b)
-    int ancL, ancO, ancR;    // anchor (centre) cells of the left / own / right chunk, -1 if none
+    int a, b;        // owned cells [a, b)
+    int anc;         // anchor cell of the chunk's frame
+    int id, idL, idR;  // this chunk's and its neighbours' ids (-1 if none), index of bsum
 };
 
 struct Frame1 {
@@ -91,32 +95,43 @@ __device__ __forceinline__ double load_state(const void* __restrict__ hi, const 
     return static_cast<const double*>(hi)[idx];
 }
 
+// boundary flux sums of one chunk over a sweep: [side 0 = left interface, 1 = right][comp],
+// each lam * sum over steps of the full flux (Fref + Delta) the chunk applied there
+struct BSum {
+    double s[2][3];
+};
+
 struct SweepArgs {
     const TubeP* tubes;
     const Chunk* chunks;
     void* hi[2];        // state planes of each buffer (double, or FP32 value)
     float* lo[2];       // FP32 compensation planes (Kahan)
+    BSum* bsum[2];      // per chunk id, by sweep parity
     long plane;         // cells per plane (all tubes)
     int sweep, B;
     int* flag;
 };
 
+// correction owed to the first owned cell of the chunk with id `right` by its left neighbour
+// `left` for the sweep whose sums are in bs: lam*sum(F_left) - lam*sum(F_right) at their interface
+__device__ __forceinline__ double boundary_correction(const BSum* bs, int left, int right, int k) {
+    return bs[left].s[1][k] - bs[right].s[0][k];
+}
+
 struct Smem1 {
-    Frame1 fr[3];
-    float sfp[3][MW], sfm[3][MW];
-    float xfp[2][3][3], xfm[2][3][3];   // [boundary][slot][comp] alternate-frame fluxes
-    float sTh[3][MW], sTl[3][MW];       // lam*Delta of interface (w, w+1), as an FP32 pair
-    float cB[2][3][2];                  // lam*(Fref_left - Fref_right) at each boundary (pair)
-    float dFr[2][3][2];                 // U*_left - U*_right at each boundary (pair)
+    Frame1 fr;
+    alignas(16) float sfp[3][MW];
+    alignas(16) float sfm[3][MW];
+    float sTh[3][MT], sTl[3][MT];       // lam*Delta of each thread's last interface (FP32 pair)
     float wall[2][3][2];                // constant wall terms (order 1) for cell 0 / n-1
+    double corr[2][3];                  // boundary corrections of cells a and b (previous sweep)
 };
 
 template <int ORDER, bool KAHAN>
 __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp, Smem1& S) {
     constexpr int R_ = ORDER;  // stencil reach per step
-    Frame1* fr = S.fr;
-    auto& sfp = S.sfp; auto& sfm = S.sfm; auto& xfp = S.xfp; auto& xfm = S.xfm;
-    auto& sTh = S.sTh; auto& sTl = S.sTl; auto& cB = S.cB; auto& dFr = S.dFr; auto& wall = S.wall;
+    Frame1& fr = S.fr;
+    auto& sfp = S.sfp; auto& sfm = S.sfm; auto& sTh = S.sTh; auto& sTl = S.sTl; auto& wall = S.wall;
 
     const int tid = threadIdx.x;
     const int n = tp.n;
@@ -124,185 +139,187 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     if (steps <= 0) return;
     const int H = R_ * steps;
     const int ws = max(0, ch.a - H), we = min(n, ch.b + H), L = we - ws;
-    const int pa = ch.a - ws, pb = ch.b - ws;  // frame boundaries in window coordinates
+    const int pa = ch.a - ws, pb = ch.b - ws;  // first owned / one past the last owned, window coords
     const int inb = (tp.par + A.sweep) & 1, outb = inb ^ 1;
     const void* hin = A.hi[inb];
     const float* lin = A.lo[inb];
     const long base = tp.base;
     const long P = A.plane;
+    const double lam = tp.lam;
+    const float lamh = (float)lam, laml = (float)(lam - (double)lamh);
 
     if (L > MW) {  // host guarantees this never happens; refuse rather than overrun
         if (tid == 0) atomicOr(A.flag, SHLL_FLAG_BADARG);
         return;
     }
-    // frames: 0 = left neighbour, 1 = own, 2 = right neighbour
-    if (tid < 3) {
-        int anc = tid == 0 ? ch.ancL : (tid == 1 ? ch.ancO : ch.ancR);
-        if (anc >= 0) {
-            double U[3];
-            for (int k = 0; k < 3; k++) U[k] = load_state<KAHAN>(hin, lin, k * P + base + anc);
-            make_frame(fr[tid], U, tp);
+    // corrections of the previous sweep for cell a (from the left neighbour) and cell b (the right
+    // neighbour's first cell, which lies in this window's halo)
+    if (tid < 6) {
+        const int side = tid / 3, k = tid % 3;
+        double c = 0.0;
+        if (A.sweep > 0) {
+            const BSum* bs = A.bsum[(A.sweep - 1) & 1];
+            if (side == 0 && ch.idL >= 0) c = boundary_correction(bs, ch.idL, ch.id, k);
+            if (side == 1 && ch.idR >= 0) c = boundary_correction(bs, ch.id, ch.idR, k);
         }
+        S.corr[side][k] = c;
     }
     __syncthreads();
-    const double lam = tp.lam;
-    const float lamh = (float)lam, laml = (float)(lam - (double)lamh);
-    if (tid < 6) {
-        int bnd = tid / 3, k = tid % 3;
-        bool has = bnd == 0 ? ch.ancL >= 0 : ch.ancR >= 0;
-        int fl = bnd == 0 ? 0 : 1, frr = bnd == 0 ? 1 : 2;
-        double c = has ? lam * (fr[fl].F[k] - fr[frr].F[k]) : 0.0;
-        double d = has ? fr[fl].U[k] - fr[frr].U[k] : 0.0;
-        split2(c, cB[bnd][k][0], cB[bnd][k][1]);
-        split2(d, dFr[bnd][k][0], dFr[bnd][k][1]);
-        // order-1 reflective walls: constant parts of the wall-cell increments
+    if (tid == 0) {
+        double U[3];
+        for (int k = 0; k < 3; k++) {
+            U[k] = load_state<KAHAN>(hin, lin, k * P + base + ch.anc);
+            if (ch.anc == ch.a) U[k] += S.corr[0][k];
+            if (ch.anc == ch.b) U[k] += S.corr[1][k];
+        }
+        make_frame(fr, U, tp);
+    }
+    __syncthreads();
+    if (tid < 6 && ORDER == 1) {
+        // reflective walls: constant parts of the wall-cell increments
         // cell 0:   lam*F_{-1/2} - lam*Fref = (-lam F0, lam (2 fmS1 - F1), -lam F2) (+2 lam dfm1_0)
         // cell n-1: lam*Fref - lam*F_{n-1/2} = (lam F0, lam (F1 - 2 fpS1), lam F2) (-2 lam dfp1_{n-1})
-        if (ORDER == 1) {
-            const Frame1& f = fr[1];
-            double w = bnd == 0 ? (k == 1 ? lam * (2.0 * f.fmS1 - f.F[1]) : -lam * f.F[k])
-                                : (k == 1 ? lam * (f.F[1] - 2.0 * f.fpS1) : lam * f.F[k]);
-            split2(w, wall[bnd][k][0], wall[bnd][k][1]);
-        }
+        const int bnd = tid / 3, k = tid % 3;
+        double w = bnd == 0 ? (k == 1 ? lam * (2.0 * fr.fmS1 - fr.F[1]) : -lam * fr.F[k])
+                            : (k == 1 ? lam * (fr.F[1] - 2.0 * fr.fpS1) : lam * fr.F[k]);
+        split2(w, wall[bnd][k][0], wall[bnd][k][1]);
     }
-    __syncthreads();
 
-    // ---- load the window as deviations from each cell's frame ----
+    // ---- load the window as deviations from the frame ----
+    const int w0 = tid * MC;
     float dh[MC][3], dl[MC][3];
 #pragma unroll
     for (int q = 0; q < MC; q++) {
-        const int w = tid * MC + q;
-        const int f = w < pa ? 0 : (w < pb ? 1 : 2);
+        const int w = w0 + q;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             dh[q][k] = 0.f; dl[q][k] = 0.f;
             if (w < L) {
                 const long idx = k * P + base + ws + w;
+                const double c = (w == pa) ? S.corr[0][k] : ((w == pb) ? S.corr[1][k] : 0.0);
                 if (KAHAN) {
-                    float h = static_cast<const float*>(hin)[idx], l = lin[idx];
-                    ff_sub(h, l, fr[f].Uh[k], fr[f].Ul[k], dh[q][k], dl[q][k]);
+                    const float h = static_cast<const float*>(hin)[idx], l = lin[idx];
+                    if (c != 0.0) {
+                        const double d = ((double)h - fr.U[k]) + (double)l + c;
+                        split2(d, dh[q][k], dl[q][k]);
+                    } else {
+                        ff_sub(h, l, fr.Uh[k], fr.Ul[k], dh[q][k], dl[q][k]);
+                    }
                 } else {
-                    double d = static_cast<const double*>(hin)[idx] - fr[f].U[k];
+                    const double d = (static_cast<const double*>(hin)[idx] + c) - fr.U[k];
                     split2(d, dh[q][k], dl[q][k]);
                 }
             }
         }
     }
+    // flux sums at the chunk's two boundary interfaces (kept by the threads that apply them)
+    float bh[2][3] = {{0, 0, 0}, {0, 0, 0}}, bl[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    const bool hasL = ch.idL >= 0, hasR = ch.idR >= 0;
 
     for (int s = 0; s < steps; s++) {
-        // ---- split-flux deviations in the cell's own frame (+ alternate frames at boundaries) ----
+        // ---- A: split-flux deviations ----
+        float fp[MC][3], fm[MC][3];
 #pragma unroll
         for (int q = 0; q < MC; q++) {
-            const int w = tid * MC + q;
-            if (w >= L) continue;
-            const int f = w < pa ? 0 : (w < pb ? 1 : 2);
-            float d[3], p3[3], m3[3];
+            float d[3];
 #pragma unroll
             for (int k = 0; k < 3; k++) d[k] = __fadd_rn(dh[q][k], dl[q][k]);
-            dflux1(fr[f].c, d, p3, m3);
+            dflux1(fr.c, d, fp[q], fm[q]);
+        }
 #pragma unroll
-            for (int k = 0; k < 3; k++) { sfp[k][w] = p3[k]; sfm[k][w] = m3[k]; }
-            // alternate frames: boundary at pa (frames 0|1) and pb (frames 1|2)
+        for (int q = 0; q < MC; q++)
 #pragma unroll
-            for (int bnd = 0; bnd < 2; bnd++) {
-                const int beta = bnd == 0 ? pa : pb;
-                const bool has = bnd == 0 ? ch.ancL >= 0 : ch.ancR >= 0;
-                if (!has) continue;
-                int slot = -1, g = 0;
-                float sgn = 1.f;
-                if (w == beta - 1) { slot = 0; g = bnd + 1; sgn = 1.f; }              // left cell in right frame
-                else if (w == beta || (ORDER == 2 && w == beta + 1)) { slot = 1 + (w - beta); g = bnd; sgn = -1.f; }
-                if (slot < 0) continue;
-                // deviation in frame g: d + (U*_f - U*_g) = d +/- (U*_left - U*_right)
-                float e[3], ap[3], am[3];
+            for (int k = 0; k < 3; k++) { sfp[k][w0 + q] = fp[q][k]; sfm[k][w0 + q] = fm[q][k]; }
+        __syncthreads();
+        // ---- B: interface terms lam*Delta_{j+1/2}, j = w0..w0+MC-1 ----
+        float th[MC][3], tl[MC][3];
+        float pl[3], pr[2][3], mr[2][3];
+        {   // neighbours' values (clamped at the window ends, whose cells are in the halo)
+            const int cl = max(w0 - 1, 0), cr0 = min(w0 + MC, MW - 1), cr1 = min(w0 + MC + 1, MW - 1);
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    float sh = __fadd_rn(dh[q][k], sgn * dFr[bnd][k][0]);
-                    float sl = __fadd_rn(dl[q][k], sgn * dFr[bnd][k][1]);
-                    e[k] = __fadd_rn(sh, sl);
-                }
-                dflux1(fr[g].c, e, ap, am);
-#pragma unroll
-                for (int k = 0; k < 3; k++) { xfp[bnd][slot][k] = ap[k]; xfm[bnd][slot][k] = am[k]; }
+            for (int k = 0; k < 3; k++) {
+                pl[k] = sfp[k][cl];
+                pr[0][k] = sfp[k][cr0]; pr[1][k] = sfp[k][cr1];
+                mr[0][k] = sfm[k][cr0]; mr[1][k] = sfm[k][cr1];
             }
         }
-        __syncthreads();
-        // ---- interface terms lam*Delta_{w+1/2} in the frame of cell w ----
-        auto gp = [&](int k, int c, int f) -> float {  // d fp of window cell c in frame f
-            c = max(0, min(L - 1, c));
-            int fc = c < pa ? 0 : (c < pb ? 1 : 2);
-            if (fc == f) return sfp[k][c];
-            if (f < fc) { int bnd = f; int beta = bnd == 0 ? pa : pb; int sl = 1 + (c - beta); sl = min(2, max(1, sl)); return xfp[bnd][sl][k]; }
-            int bnd = fc; return xfp[bnd][0][k];
-        };
-        auto gm = [&](int k, int c, int f) -> float {
-            c = max(0, min(L - 1, c));
-            int fc = c < pa ? 0 : (c < pb ? 1 : 2);
-            if (fc == f) return sfm[k][c];
-            if (f < fc) { int bnd = f; int beta = bnd == 0 ? pa : pb; int sl = 1 + (c - beta); sl = min(2, max(1, sl)); return xfm[bnd][sl][k]; }
-            int bnd = fc; return xfm[bnd][0][k];
-        };
 #pragma unroll
         for (int q = 0; q < MC; q++) {
-            const int w = tid * MC + q;
-            if (w >= L - 1) continue;
-            const int i = ws + w;  // tube cell
-            const int f = w < pa ? 0 : (w < pb ? 1 : 2);
+            const int i = ws + w0 + q;  // tube cell of interface (i, i+1)
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 float Dl;
+                const float p1 = fp[q][k];
+                const float m2 = q + 1 < MC ? fm[q + 1][k] : mr[0][k];
                 if (ORDER == 1) {
-                    Dl = __fadd_rn(gp(k, w, f), gm(k, w + 1, f));
+                    Dl = __fadd_rn(p1, m2);
                 } else {
-                    float p0 = gp(k, w - 1, f), p1 = gp(k, w, f), p2 = gp(k, w + 1, f);
-                    float m1 = gm(k, w, f), m2 = gm(k, w + 1, f), m3 = gm(k, w + 2, f);
-                    float sp = (i == 0 || i == n - 1) ? 0.f : slope_f(p0, p1, p2, tp.limiter, tp.alpha);
-                    float sm = (i + 1 == n - 1) ? 0.f : slope_f(m1, m2, m3, tp.limiter, tp.alpha);
+                    const float p0 = q > 0 ? fp[q - 1][k] : pl[k];
+                    const float p2 = q + 1 < MC ? fp[q + 1][k] : pr[0][k];
+                    const float m1 = fm[q][k];
+                    const float m3 = q + 2 < MC ? fm[q + 2][k] : mr[q + 2 - MC][k];
+                    const float sp = (i == 0 || i == n - 1) ? 0.f : slope_f(p0, p1, p2, tp.limiter, tp.alpha);
+                    const float sm = (i + 1 == n - 1) ? 0.f : slope_f(m1, m2, m3, tp.limiter, tp.alpha);
                     Dl = __fadd_rn(__fadd_rn(__fadd_rn(p1, __fmul_rn(0.5f, sp)), m2), -__fmul_rn(0.5f, sm));
                 }
-                float th = __fmul_rn(lamh, Dl);
-                float tl = __fadd_rn(__fmaf_rn(lamh, Dl, -th), __fmul_rn(laml, Dl));
-                sTh[k][w] = th; sTl[k][w] = tl;
+                th[q][k] = __fmul_rn(lamh, Dl);
+                tl[q][k] = __fadd_rn(__fmaf_rn(lamh, Dl, -th[q][k]), __fmul_rn(laml, Dl));
             }
         }
+#pragma unroll
+        for (int k = 0; k < 3; k++) { sTh[k][tid] = th[MC - 1][k]; sTl[k][tid] = tl[MC - 1][k]; }
         __syncthreads();
-        // ---- accumulate: lam*(F_{i-1/2} - F_{i+1/2}) per cell ----
+        // ---- C: accumulate lam*(F_{i-1/2} - F_{i+1/2}) per cell ----
 #pragma unroll
         for (int q = 0; q < MC; q++) {
-            const int w = tid * MC + q;
-            if (w >= L) continue;
+            const int w = w0 + q;
             const int i = ws + w;
+            if (w >= L) continue;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 float& h = dh[q][k];
                 float& l = dl[q][k];
-                if (i > 0 && w > 0) { two_sum_acc(h, l, sTh[k][w - 1]); l = __fadd_rn(l, sTl[k][w - 1]); }
-                if (i < n - 1 && w < L - 1) { two_sum_acc(h, l, -sTh[k][w]); l = __fadd_rn(l, -sTl[k][w]); }
-                if (w > 0 && (w == pa || w == pb)) {  // left neighbour in another frame
-                    const int bnd = w == pa ? 0 : 1;
-                    two_sum_acc(h, l, cB[bnd][k][0]); l = __fadd_rn(l, cB[bnd][k][1]);
+                if (i > 0 && w > 0) {
+                    const float ih = q > 0 ? th[q - 1][k] : sTh[k][max(tid - 1, 0)];
+                    const float il = q > 0 ? tl[q - 1][k] : sTl[k][max(tid - 1, 0)];
+                    two_sum_acc(h, l, ih); l = __fadd_rn(l, il);
+                    if (w == pa && hasL) { two_sum_acc(bh[0][k], bl[0][k], ih); bl[0][k] = __fadd_rn(bl[0][k], il); }
+                }
+                if (i < n - 1 && w < L - 1) {
+                    two_sum_acc(h, l, -th[q][k]); l = __fadd_rn(l, -tl[q][k]);
+                    if (w == pb - 1 && hasR) { two_sum_acc(bh[1][k], bl[1][k], th[q][k]); bl[1][k] = __fadd_rn(bl[1][k], tl[q][k]); }
                 }
                 if (i == 0 || i == n - 1) {
                     if (ORDER == 1) {
                         const int bnd = i == 0 ? 0 : 1;
                         two_sum_acc(h, l, wall[bnd][k][0]); l = __fadd_rn(l, wall[bnd][k][1]);
                         if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
-                            float v = i == 0 ? __fmul_rn(2.f, sfm[1][w]) : -__fmul_rn(2.f, sfp[1][w]);
-                            float vh = __fmul_rn(lamh, v);
-                            float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
+                            const float v = i == 0 ? __fmul_rn(2.f, fm[q][1]) : -__fmul_rn(2.f, fp[q][1]);
+                            const float vh = __fmul_rn(lamh, v);
+                            const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
                             two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                         }
                     } else {  // outflow: F_{-1/2} = Fref + dfp_0 + dfm_0 (and likewise at n-1)
-                        float v = __fadd_rn(sfp[k][w], sfm[k][w]);
+                        float v = __fadd_rn(fp[q][k], fm[q][k]);
                         if (i == n - 1) v = -v;
-                        float vh = __fmul_rn(lamh, v);
-                        float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
+                        const float vh = __fmul_rn(lamh, v);
+                        const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
                         two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                     }
                 }
             }
         }
-        __syncthreads();
+    }
+    // ---- boundary flux sums of this sweep (full flux: steps * lam * Fref + sum lam*Delta) ----
+    BSum* bout = A.bsum[A.sweep & 1] + ch.id;
+#pragma unroll
+    for (int q = 0; q < MC; q++) {
+        const int w = w0 + q;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (w == pa && hasL) bout->s[0][k] = steps * lam * fr.F[k] + ((double)bh[0][k] + (double)bl[0][k]);
+            if (w == pb - 1 && hasR) bout->s[1][k] = steps * lam * fr.F[k] + ((double)bh[1][k] + (double)bl[1][k]);
+        }
     }
 
     // ---- fold the owned cells into the stored state ----
@@ -311,7 +328,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     float* lout = A.lo[outb];
 #pragma unroll
     for (int q = 0; q < MC; q++) {
-        const int w = tid * MC + q;
+        const int w = w0 + q;
         if (w < pa || w >= pb) continue;
         double uu[3];
 #pragma unroll
@@ -319,18 +336,18 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             const long idx = k * P + base + ws + w;
             if (KAHAN) {
                 float oh, ol;
-                ff_add(fr[1].Uh[k], fr[1].Ul[k], dh[q][k], dl[q][k], oh, ol);
+                ff_add(fr.Uh[k], fr.Ul[k], dh[q][k], dl[q][k], oh, ol);
                 static_cast<float*>(hout)[idx] = oh;
                 lout[idx] = ol;
                 uu[k] = (double)oh;
             } else {
-                double v = fr[1].U[k] + ((double)dh[q][k] + (double)dl[q][k]);
+                const double v = fr.U[k] + ((double)dh[q][k] + (double)dl[q][k]);
                 static_cast<double*>(hout)[idx] = v;
                 uu[k] = v;
             }
         }
-        float r = (float)uu[0], m = (float)uu[1], E = (float)uu[2];
-        float eint = __fadd_rn(E, -__fmul_rn(0.5f, __fdividef(__fmul_rn(m, m), r)));
+        const float r = (float)uu[0], m = (float)uu[1], E = (float)uu[2];
+        const float eint = __fadd_rn(E, -__fmul_rn(0.5f, __fdividef(__fmul_rn(m, m), r)));
         bad |= !(r > 0.f) || !(eint > 0.f);
     }
     if (bad) atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
@@ -343,6 +360,32 @@ __global__ void __launch_bounds__(MT) k_sweep1d(SweepArgs A) {
     const TubeP tp = A.tubes[ch.tube];
     if (tp.order == 2) sweep_chunk<2, KAHAN>(A, ch, tp, S);
     else sweep_chunk<1, KAHAN>(A, ch, tp, S);
+}
+
+// Applies the last sweep's boundary corrections of a run to the first owned cell of every chunk
+// that has a left neighbour (the state buffer that holds the tube after the run).
+template <bool KAHAN>
+__global__ void k_fixup1d(SweepArgs A, int nchunks) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const Chunk ch = A.chunks[c];
+    const TubeP tp = A.tubes[ch.tube];
+    if (ch.idL < 0 || tp.steps <= 0) return;
+    const int sweeps = (tp.steps + A.B - 1) / A.B;
+    const BSum* bs = A.bsum[(sweeps - 1) & 1];
+    const int buf = (tp.par + sweeps) & 1;
+    for (int k = 0; k < 3; k++) {
+        const long idx = k * A.plane + tp.base + ch.a;
+        const double corr = boundary_correction(bs, ch.idL, ch.id, k);
+        if (KAHAN) {
+            float* h = static_cast<float*>(A.hi[buf]);
+            float* l = A.lo[buf];
+            const double v = ((double)h[idx] + (double)l[idx]) + corr;
+            split2(v, h[idx], l[idx]);
+        } else {
+            static_cast<double*>(A.hi[buf])[idx] += corr;
+        }
+    }
 }
 
 }  // namespace
@@ -363,6 +406,7 @@ struct MixedState {
     Chunk* d_chunks = nullptr;
     std::vector<Chunk> chunks;         // sorted by the steps of their tube (descending)
     int* d_flag = nullptr;
+    BSum* bsum[2] = {nullptr, nullptr};  // boundary flux sums per chunk id, by sweep parity
     long cell_updates = 0;
     // device checkpoint (shll_checkpoint)
     void* ck_hi[2] = {nullptr, nullptr};
@@ -373,7 +417,16 @@ struct MixedState {
     void* d2 = nullptr;
 };
 
-static int chunk_owned(int order, int B) { return MW - 2 * order * B; }
+// owned cells per chunk: the window (MW) minus the halo on both sides; SHLL_MIXED_CHUNK (cells)
+// may lower it to put more CTAs on each SM
+static int chunk_owned(int order, int B) {
+    int S = MW - 2 * order * B;
+    if (const char* e = getenv("SHLL_MIXED_CHUNK")) {
+        int v = atoi(e);
+        if (v >= 4 * order * B && v < S) S = v;
+    }
+    return S;
+}
 
 // Chunks of every tube.  A tube has at least two chunks; the first chunk's frame is anchored
 // at the left wall cell and the last chunk's at the right wall cell, so that a wall region
@@ -390,8 +443,10 @@ static void build_chunks(MixedState* m) {
         std::vector<int> edges(k + 1), anc(k);
         for (int c = 0; c <= k; c++) edges[c] = (int)((long)n * c / k);
         for (int c = 0; c < k; c++) anc[c] = c == 0 ? 0 : (c == k - 1 ? n - 1 : (edges[c] + edges[c + 1]) / 2);
+        const int id0 = (int)m->chunks.size();
         for (int c = 0; c < k; c++)
-            m->chunks.push_back({t, edges[c], edges[c + 1], c > 0 ? anc[c - 1] : -1, anc[c], c + 1 < k ? anc[c + 1] : -1});
+            m->chunks.push_back({t, edges[c], edges[c + 1], anc[c], id0 + c, c > 0 ? id0 + c - 1 : -1,
+                                 c + 1 < k ? id0 + c + 1 : -1});
     }
 }
 
@@ -404,6 +459,13 @@ static int alloc_mixed(MixedState* m, char* err, size_t len) {
         }
         if (m->kahan && cudaMalloc(&m->lo[b], cells * sizeof(float)) != cudaSuccess) {
             snprintf(err, len, "cudaMalloc of compensation planes failed");
+            return SHLL_ERR_NOMEM;
+        }
+    }
+    for (int b = 0; b < 2; b++) {
+        if (cudaMalloc(&m->bsum[b], sizeof(BSum) * m->chunks.size()) != cudaSuccess ||
+            cudaMemset(m->bsum[b], 0, sizeof(BSum) * m->chunks.size()) != cudaSuccess) {
+            snprintf(err, len, "cudaMalloc of boundary sums failed");
             return SHLL_ERR_NOMEM;
         }
     }
@@ -504,6 +566,8 @@ void mixed_destroy(MixedState* m) {
     }
     cudaFree(m->d_tubes);
     cudaFree(m->d_chunks);
+    cudaFree(m->bsum[0]);
+    cudaFree(m->bsum[1]);
     cudaFree(m->d_flag);
     delete m;
 }
@@ -607,15 +671,20 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     A.chunks = m->d_chunks;
     A.hi[0] = m->hi[0]; A.hi[1] = m->hi[1];
     A.lo[0] = m->lo[0]; A.lo[1] = m->lo[1];
+    A.bsum[0] = m->bsum[0]; A.bsum[1] = m->bsum[1];
     A.plane = m->plane;
     A.B = m->B;
     A.flag = m->d_flag;
-    shll_count_launches(nsweeps);
+    A.sweep = 0;
+    shll_count_launches(nsweeps + 1);
     for (long k = 0; k < nsweeps; k++) {
         A.sweep = (int)k;
         if (m->kahan) k_sweep1d<true><<<active[k], MT, 0, m->stream>>>(A);
         else k_sweep1d<false><<<active[k], MT, 0, m->stream>>>(A);
     }
+    const int nch = (int)order.size();
+    if (m->kahan) k_fixup1d<true><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);
+    else k_fixup1d<false><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { snprintf(err, len, "sweep launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     for (int t = 0; t < m->nitems; t++) {
