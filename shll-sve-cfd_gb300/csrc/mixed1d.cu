@@ -48,6 +48,7 @@ struct TubeP {
     int par;          // buffer holding the tube's state at the start of the run
     double gamma, R, CV, lam;
     float alpha;
+    int lam_pow2;     // lam is a power of two: lam*Delta is exact in FP32
 };
 
 struct Chunk {
@@ -127,7 +128,7 @@ struct Smem1 {
     double corr[2][3];                  // boundary corrections of cells a and b (previous sweep)
 };
 
-template <int ORDER, bool KAHAN>
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
 __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp, Smem1& S) {
     constexpr int R_ = ORDER;  // stencil reach per step
     Frame1& fr = S.fr;
@@ -141,8 +142,9 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     const int ws = max(0, ch.a - H), we = min(n, ch.b + H), L = we - ws;
     const int pa = ch.a - ws, pb = ch.b - ws;  // first owned / one past the last owned, window coords
     const int inb = (tp.par + A.sweep) & 1, outb = inb ^ 1;
-    const void* hin = A.hi[inb];
-    const float* lin = A.lo[inb];
+    // (selects rather than indexing the parameter arrays, which would copy them to local memory)
+    const void* hin = inb ? A.hi[1] : A.hi[0];
+    const float* lin = inb ? A.lo[1] : A.lo[0];
     const long base = tp.base;
     const long P = A.plane;
     const double lam = tp.lam;
@@ -158,7 +160,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         const int side = tid / 3, k = tid % 3;
         double c = 0.0;
         if (A.sweep > 0) {
-            const BSum* bs = A.bsum[(A.sweep - 1) & 1];
+            const BSum* bs = ((A.sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
             if (side == 0 && ch.idL >= 0) c = boundary_correction(bs, ch.idL, ch.id, k);
             if (side == 1 && ch.idR >= 0) c = boundary_correction(bs, ch.id, ch.idR, k);
         }
@@ -196,17 +198,18 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             dh[q][k] = 0.f; dl[q][k] = 0.f;
             if (w < L) {
                 const long idx = k * P + base + ws + w;
-                const double c = (w == pa) ? S.corr[0][k] : ((w == pb) ? S.corr[1][k] : 0.0);
+                const bool corrected = w == pa || w == pb;  // cells owed a boundary correction
                 if (KAHAN) {
                     const float h = static_cast<const float*>(hin)[idx], l = lin[idx];
-                    if (c != 0.0) {
-                        const double d = ((double)h - fr.U[k]) + (double)l + c;
+                    if (corrected) {
+                        const double d = ((double)h - fr.U[k]) + (double)l + S.corr[w == pa ? 0 : 1][k];
                         split2(d, dh[q][k], dl[q][k]);
                     } else {
                         ff_sub(h, l, fr.Uh[k], fr.Ul[k], dh[q][k], dl[q][k]);
                     }
                 } else {
-                    const double d = (static_cast<const double*>(hin)[idx] + c) - fr.U[k];
+                    double d = static_cast<const double*>(hin)[idx] - fr.U[k];
+                    if (corrected) d += S.corr[w == pa ? 0 : 1][k];
                     split2(d, dh[q][k], dl[q][k]);
                 }
             }
@@ -215,6 +218,17 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     // flux sums at the chunk's two boundary interfaces (kept by the threads that apply them)
     float bh[2][3] = {{0, 0, 0}, {0, 0, 0}}, bl[2][3] = {{0, 0, 0}, {0, 0, 0}};
     const bool hasL = ch.idL >= 0, hasR = ch.idR >= 0;
+    // loop-invariant roles of this thread's cells
+    bool in_ok[MC], out_ok[MC], sp0[MC], sm0[MC], special[MC];
+#pragma unroll
+    for (int q = 0; q < MC; q++) {
+        const int w = w0 + q, i = ws + w;
+        in_ok[q] = i > 0 && w > 0 && w < L;
+        out_ok[q] = i < n - 1 && w < L - 1;
+        sp0[q] = i == 0 || i == n - 1;          // dfp of cell i is zero (edge cell)
+        sm0[q] = i + 1 == n - 1;                // dfm of cell i+1 is zero
+        special[q] = w < L && (i == 0 || i == n - 1 || (w == pa && hasL) || (w == pb - 1 && hasR));
+    }
 
     for (int s = 0; s < steps; s++) {
         // ---- A: split-flux deviations ----
@@ -238,14 +252,12 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             const int cl = max(w0 - 1, 0), cr0 = min(w0 + MC, MW - 1), cr1 = min(w0 + MC + 1, MW - 1);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                pl[k] = sfp[k][cl];
-                pr[0][k] = sfp[k][cr0]; pr[1][k] = sfp[k][cr1];
-                mr[0][k] = sfm[k][cr0]; mr[1][k] = sfm[k][cr1];
+                if (ORDER == 2) { pl[k] = sfp[k][cl]; pr[0][k] = sfp[k][cr0]; mr[1][k] = sfm[k][cr1]; }
+                mr[0][k] = sfm[k][cr0];
             }
         }
 #pragma unroll
         for (int q = 0; q < MC; q++) {
-            const int i = ws + w0 + q;  // tube cell of interface (i, i+1)
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 float Dl;
@@ -258,60 +270,65 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                     const float p2 = q + 1 < MC ? fp[q + 1][k] : pr[0][k];
                     const float m1 = fm[q][k];
                     const float m3 = q + 2 < MC ? fm[q + 2][k] : mr[q + 2 - MC][k];
-                    const float sp = (i == 0 || i == n - 1) ? 0.f : slope_f(p0, p1, p2, tp.limiter, tp.alpha);
-                    const float sm = (i + 1 == n - 1) ? 0.f : slope_f(m1, m2, m3, tp.limiter, tp.alpha);
+                    const float sp = sp0[q] ? 0.f : slope_f<LIM>(p0, p1, p2, tp.alpha);
+                    const float sm = sm0[q] ? 0.f : slope_f<LIM>(m1, m2, m3, tp.alpha);
                     Dl = __fadd_rn(__fadd_rn(__fadd_rn(p1, __fmul_rn(0.5f, sp)), m2), -__fmul_rn(0.5f, sm));
                 }
                 th[q][k] = __fmul_rn(lamh, Dl);
-                tl[q][k] = __fadd_rn(__fmaf_rn(lamh, Dl, -th[q][k]), __fmul_rn(laml, Dl));
+                tl[q][k] = LAM_POW2 ? 0.f : __fadd_rn(__fmaf_rn(lamh, Dl, -th[q][k]), __fmul_rn(laml, Dl));
             }
         }
 #pragma unroll
-        for (int k = 0; k < 3; k++) { sTh[k][tid] = th[MC - 1][k]; sTl[k][tid] = tl[MC - 1][k]; }
+        for (int k = 0; k < 3; k++) {
+            sTh[k][tid] = th[MC - 1][k];
+            if (!LAM_POW2) sTl[k][tid] = tl[MC - 1][k];
+        }
         __syncthreads();
         // ---- C: accumulate lam*(F_{i-1/2} - F_{i+1/2}) per cell ----
+        const int tl_ = max(tid - 1, 0);
 #pragma unroll
         for (int q = 0; q < MC; q++) {
-            const int w = w0 + q;
-            const int i = ws + w;
-            if (w >= L) continue;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                float& h = dh[q][k];
-                float& l = dl[q][k];
-                if (i > 0 && w > 0) {
-                    const float ih = q > 0 ? th[q - 1][k] : sTh[k][max(tid - 1, 0)];
-                    const float il = q > 0 ? tl[q - 1][k] : sTl[k][max(tid - 1, 0)];
-                    two_sum_acc(h, l, ih); l = __fadd_rn(l, il);
+                float ih = q > 0 ? th[q - 1][k] : sTh[k][tl_];
+                float il = LAM_POW2 ? 0.f : (q > 0 ? tl[q - 1][k] : sTl[k][tl_]);
+                ih = in_ok[q] ? ih : 0.f;
+                il = in_ok[q] ? il : 0.f;
+                const float oh = out_ok[q] ? th[q][k] : 0.f;
+                const float ol = out_ok[q] ? tl[q][k] : 0.f;
+                two_sum_acc(dh[q][k], dl[q][k], ih);
+                two_sum_acc(dh[q][k], dl[q][k], -oh);
+                if (!LAM_POW2) dl[q][k] = __fadd_rn(dl[q][k], __fadd_rn(il, -ol));
+                if (special[q]) {
+                    const int w = w0 + q, i = ws + w;
+                    float& h = dh[q][k];
+                    float& l = dl[q][k];
                     if (w == pa && hasL) { two_sum_acc(bh[0][k], bl[0][k], ih); bl[0][k] = __fadd_rn(bl[0][k], il); }
-                }
-                if (i < n - 1 && w < L - 1) {
-                    two_sum_acc(h, l, -th[q][k]); l = __fadd_rn(l, -tl[q][k]);
-                    if (w == pb - 1 && hasR) { two_sum_acc(bh[1][k], bl[1][k], th[q][k]); bl[1][k] = __fadd_rn(bl[1][k], tl[q][k]); }
-                }
-                if (i == 0 || i == n - 1) {
-                    if (ORDER == 1) {
-                        const int bnd = i == 0 ? 0 : 1;
-                        two_sum_acc(h, l, wall[bnd][k][0]); l = __fadd_rn(l, wall[bnd][k][1]);
-                        if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
-                            const float v = i == 0 ? __fmul_rn(2.f, fm[q][1]) : -__fmul_rn(2.f, fp[q][1]);
+                    if (w == pb - 1 && hasR) { two_sum_acc(bh[1][k], bl[1][k], oh); bl[1][k] = __fadd_rn(bl[1][k], ol); }
+                    if (i == 0 || i == n - 1) {
+                        if (ORDER == 1) {
+                            const int bnd = i == 0 ? 0 : 1;
+                            two_sum_acc(h, l, wall[bnd][k][0]); l = __fadd_rn(l, wall[bnd][k][1]);
+                            if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
+                                const float v = i == 0 ? __fmul_rn(2.f, fm[q][1]) : -__fmul_rn(2.f, fp[q][1]);
+                                const float vh = __fmul_rn(lamh, v);
+                                const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
+                                two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
+                            }
+                        } else {  // outflow: F_{-1/2} = Fref + dfp_0 + dfm_0 (and likewise at n-1)
+                            float v = __fadd_rn(fp[q][k], fm[q][k]);
+                            if (i == n - 1) v = -v;
                             const float vh = __fmul_rn(lamh, v);
                             const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
                             two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                         }
-                    } else {  // outflow: F_{-1/2} = Fref + dfp_0 + dfm_0 (and likewise at n-1)
-                        float v = __fadd_rn(fp[q][k], fm[q][k]);
-                        if (i == n - 1) v = -v;
-                        const float vh = __fmul_rn(lamh, v);
-                        const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
-                        two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                     }
                 }
             }
         }
     }
     // ---- boundary flux sums of this sweep (full flux: steps * lam * Fref + sum lam*Delta) ----
-    BSum* bout = A.bsum[A.sweep & 1] + ch.id;
+    BSum* bout = ((A.sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
 #pragma unroll
     for (int q = 0; q < MC; q++) {
         const int w = w0 + q;
@@ -324,8 +341,8 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
 
     // ---- fold the owned cells into the stored state ----
     int bad = 0;
-    void* hout = A.hi[outb];
-    float* lout = A.lo[outb];
+    void* hout = outb ? A.hi[1] : A.hi[0];
+    float* lout = outb ? A.lo[1] : A.lo[0];
 #pragma unroll
     for (int q = 0; q < MC; q++) {
         const int w = w0 + q;
@@ -358,8 +375,19 @@ __global__ void __launch_bounds__(MT) k_sweep1d(SweepArgs A) {
     __shared__ Smem1 S;
     const Chunk ch = A.chunks[blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];
-    if (tp.order == 2) sweep_chunk<2, KAHAN>(A, ch, tp, S);
-    else sweep_chunk<1, KAHAN>(A, ch, tp, S);
+    const bool pow2 = tp.lam_pow2;
+    if (tp.order == 2) {
+        if (tp.limiter == 1) {
+            if (pow2) sweep_chunk<2, KAHAN, true, 1>(A, ch, tp, S);
+            else sweep_chunk<2, KAHAN, false, 1>(A, ch, tp, S);
+        } else {
+            if (pow2) sweep_chunk<2, KAHAN, true, 0>(A, ch, tp, S);
+            else sweep_chunk<2, KAHAN, false, 0>(A, ch, tp, S);
+        }
+    } else {
+        if (pow2) sweep_chunk<1, KAHAN, true, 0>(A, ch, tp, S);
+        else sweep_chunk<1, KAHAN, false, 0>(A, ch, tp, S);
+    }
 }
 
 // Applies the last sweep's boundary corrections of a run to the first owned cell of every chunk
@@ -372,18 +400,18 @@ __global__ void k_fixup1d(SweepArgs A, int nchunks) {
     const TubeP tp = A.tubes[ch.tube];
     if (ch.idL < 0 || tp.steps <= 0) return;
     const int sweeps = (tp.steps + A.B - 1) / A.B;
-    const BSum* bs = A.bsum[(sweeps - 1) & 1];
+    const BSum* bs = ((sweeps - 1) & 1) ? A.bsum[1] : A.bsum[0];
     const int buf = (tp.par + sweeps) & 1;
     for (int k = 0; k < 3; k++) {
         const long idx = k * A.plane + tp.base + ch.a;
         const double corr = boundary_correction(bs, ch.idL, ch.id, k);
         if (KAHAN) {
-            float* h = static_cast<float*>(A.hi[buf]);
-            float* l = A.lo[buf];
+            float* h = static_cast<float*>(buf ? A.hi[1] : A.hi[0]);
+            float* l = buf ? A.lo[1] : A.lo[0];
             const double v = ((double)h[idx] + (double)l[idx]) + corr;
             split2(v, h[idx], l[idx]);
         } else {
-            static_cast<double*>(A.hi[buf])[idx] += corr;
+            static_cast<double*>(buf ? A.hi[1] : A.hi[0])[idx] += corr;
         }
     }
 }
@@ -537,6 +565,10 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
         double lamy;
         item_consts(p, &tp.CV, &tp.lam, &lamy);
         tp.alpha = (float)p.mc_alpha;
+        {
+            int ex;
+            tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
+        }
         tp.steps = 0;
         tp.par = 0;
         m->tubes.push_back(tp);

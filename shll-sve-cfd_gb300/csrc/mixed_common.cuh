@@ -50,11 +50,12 @@ __device__ __forceinline__ float minmod_f(float l, float r) {
     if (__fmul_rn(l, r) < 0.f) return 0.f;
     return fabsf(l) < fabsf(r) ? l : r;
 }
-// limited slope from three consecutive values: minmod, or the MC limiter
-// (base-omp/2nd_order_base_shll.c:316-325)
-__device__ __forceinline__ float slope_f(float fl, float fc, float fr, int limiter, float alpha) {
+// limited slope from three consecutive values: minmod (LIM = 0), or the MC limiter (LIM = 1,
+// base-omp/2nd_order_base_shll.c:316-325)
+template <int LIM>
+__device__ __forceinline__ float slope_f(float fl, float fc, float fr, float alpha) {
     float a = __fadd_rn(fc, -fl), b = __fadd_rn(fr, -fc);
-    if (limiter == 1) return minmod_f(__fmul_rn(0.5f, __fadd_rn(fr, -fl)), __fmul_rn(alpha, minmod_f(a, b)));
+    if (LIM == 1) return minmod_f(__fmul_rn(0.5f, __fadd_rn(fr, -fl)), __fmul_rn(alpha, minmod_f(a, b)));
     return minmod_f(a, b);
 }
 
@@ -71,9 +72,11 @@ __device__ __forceinline__ void dflux1(const AnchorCoef& c, const float d[3], fl
     const float de = __fmul_rn(__fmaf_rn(-c.e, drho, dE), r);
     const float dT = __fmul_rn(__fmaf_rn(-0.5f * 1.0f, __fmul_rn(__fadd_rn(u, c.u), du), de), c.cvinv);
     const float T = __fadd_rn(c.T, dT);
-    const float a = fast_sqrt(__fmul_rn(c.gR, T));
+    const float gRT = __fmul_rn(c.gR, T);
+    const float ainv = rsqrtf(gRT);           // 1/a
+    const float a = __fmul_rn(gRT, ainv);     // a = sqrt(gamma R T)
     const float da = __fmul_rn(__fmul_rn(c.gR, dT), fast_rcp(__fadd_rn(a, c.a)));
-    const float dM = __fmul_rn(__fmaf_rn(-c.M, da, du), fast_rcp(a));
+    const float dM = __fmul_rn(__fmaf_rn(-c.M, da, du), ainv);
     const float M = __fadd_rn(c.M, dM);
     const float dZ1 = __fmul_rn(0.5f, dM);
     const float Z1 = __fadd_rn(c.Z1, dZ1);
