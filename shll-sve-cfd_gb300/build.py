@@ -66,6 +66,15 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    # the reference-style C driver (host code in C over the C-ABI)
+    drv = os.path.join(BUILD, "shll_tube")
+    src = os.path.join(HERE, "host", "shll_tube.c")
+    if _stale(drv, [src, LIB]):
+        cmd = ["gcc", "-O2", "-Wall", "-I", os.path.join(HERE, "..", "include"), src, "-o", drv,
+               "-L", BUILD, "-lshll_gb300", f"-Wl,-rpath,{BUILD}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stderr}")
     return LIB
 
 
