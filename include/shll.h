@@ -173,6 +173,23 @@ long shll_batch_cell_updates(const shll_batch* b);
 const char* shll_batch_last_error(const shll_batch* b);
 void shll_batch_destroy(shll_batch* b);
 
+/* ---- advancing a tube without allocating device memory ----
+ * No counterpart in the reference (which has no GPU path).  For callers that cannot call
+ * cudaMalloc when they need to step: a process whose device allocator is reserved or capped by
+ * its host framework, a time-critical loop that must not wait on the allocator, or a host that
+ * hands the library device buffers it manages itself.  d_cons is the caller's device buffer of
+ * the tube's conserved variables (planes rho, rho*u, E of p->nx doubles each); it is advanced in
+ * place by nsteps steps (nsteps <= 0: the whole run of shll_steps_for(p)) with the
+ * SHLL_PREC_MIXED_F64 arithmetic of shll_step, on `stream` (a cudaStream_t, NULL = default).
+ * All other memory it needs lives in one 2 MiB array inside the library, which every GPU that
+ * loads the library holds until the process exits; so p->nx is limited to 65536 cells (larger
+ * tubes are rejected with SHLL_ERR_ARG), p->dim must be 1 and p->precision MIXED_F64.  The first
+ * call on each device looks up that array's device address: make it before any stream capture.
+ * Every call uses the same array and leaves its contents behind, so calls that overlap on the
+ * GPU (other threads, other streams) race with each other; serialise them.  Returns after the
+ * work has completed. */
+int shll_tube_run_static(const shll_params* p, double* d_cons, long nsteps, void* stream);
+
 /* ---- the reference's own entry points on a process-wide default context ----
  * shll_ref_configure() chooses the problem (else base_shll.c's defaults, N = 256, F64). */
 int shll_ref_configure(const shll_params* p);

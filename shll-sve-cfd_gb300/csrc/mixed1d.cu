@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "mixed.h"
@@ -850,5 +851,164 @@ int mixed_checkpoint(MixedState* m, bool restore, char* err, size_t len) {
     }
     if (restore) { m->par = m->ck_par; m->cell_updates = m->ck_updates; }
     else { m->ck_par = m->par; m->ck_updates = m->cell_updates; }
+    return SHLL_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Entry point for callers that cannot allocate device memory.
+//
+// Some host programs cannot call cudaMalloc at the point where they want to advance a tube: an
+// allocator that the process has reserved or capped for itself, a real-time loop that must not
+// take the allocator's locks, or a host that hands the library device buffers it manages
+// itself.  shll_tube_run_static() advances one 1D tube held in the caller's device buffer with
+// the same sweep kernels as the context API, and keeps everything else it needs (the second
+// state buffer, the boundary flux sums, the chunk descriptors and the error flag) in the
+// fixed array below.  That array is part of the library image: every GPU that loads the library
+// holds its 2 MiB until the process exits.
+namespace {
+constexpr int kStaticMaxCells = 65536;                 // largest tube the static scratch can hold
+constexpr int kStaticMaxChunks = 256;
+constexpr size_t kStaticStateBytes = (size_t)3 * kStaticMaxCells * sizeof(double);
+constexpr size_t kStaticBSumOff = kStaticStateBytes;                                  // 2 x BSum[256]
+constexpr size_t kStaticChunkOff = kStaticBSumOff + 2 * kStaticMaxChunks * sizeof(BSum);
+constexpr size_t kStaticTubeOff = (kStaticChunkOff + kStaticMaxChunks * sizeof(Chunk) + 255) / 256 * 256;
+constexpr size_t kStaticFlagOff = kStaticTubeOff + 256;
+constexpr size_t kStaticScratchBytes = 2u << 20;
+static_assert(kStaticFlagOff + 256 <= kStaticScratchBytes, "static scratch layout exceeds its array");
+constexpr int kStaticMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+static std::mutex g_static_mu;
+static void* g_static_addr[kStaticMaxDevices];  // device address of g_static_scratch, per device
+
+// The device address of the scratch array on the current device, looked up once per device.
+// The host-side name g_static_scratch is only a stand-in: a kernel must be given this address.
+static int static_scratch(void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kStaticMaxDevices) {
+        fprintf(stderr, "shll_tube_run_static: no usable current device (%s)\n", cudaGetErrorString(e));
+        return SHLL_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p) {
+            fprintf(stderr, "shll_tube_run_static: cudaGetSymbolAddress failed on device %d: %s\n", dev,
+                    cudaGetErrorString(e));
+            return SHLL_ERR_CUDA;
+        }
+        g_static_addr[dev] = p;
+    }
+    *out = g_static_addr[dev];
+    return SHLL_OK;
+}
+
+extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long nsteps, void* stream) {
+    if (!p || !d_cons) {
+        fprintf(stderr, "shll_tube_run_static: params and state buffer are required\n");
+        return SHLL_ERR_ARG;
+    }
+    if (p->dim != 1 || (p->order != 1 && p->order != 2) || p->precision != SHLL_PREC_MIXED_F64) {
+        fprintf(stderr, "shll_tube_run_static: takes one 1D tube (order 1 or 2) in SHLL_PREC_MIXED_F64\n");
+        return SHLL_ERR_ARG;
+    }
+    if (p->nx < 2 || p->nx > kStaticMaxCells) {
+        fprintf(stderr, "shll_tube_run_static: %d cells is outside 2..%d, the size of the static scratch\n", p->nx,
+                kStaticMaxCells);
+        return SHLL_ERR_ARG;
+    }
+    if (reinterpret_cast<uintptr_t>(d_cons) % alignof(double) != 0) {
+        fprintf(stderr, "shll_tube_run_static: state buffer is not 8-byte aligned\n");
+        return SHLL_ERR_ARG;
+    }
+    if (nsteps <= 0) nsteps = shll_steps_for(p);
+    if (nsteps <= 0 || nsteps > (1L << 30)) {
+        fprintf(stderr, "shll_tube_run_static: invalid step count\n");
+        return SHLL_ERR_ARG;
+    }
+    void* base = nullptr;
+    int rc = static_scratch(&base);
+    if (rc != SHLL_OK) return rc;
+    unsigned char* sc = static_cast<unsigned char*>(base);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    // descriptors of the tube, built on the stack
+    const int fold = p->fold_steps > 0 ? p->fold_steps : 16;
+    const int B = std::min(fold, MW / 16);
+    TubeP tp;
+    memset(&tp, 0, sizeof(tp));
+    tp.base = 0;
+    tp.n = p->nx;
+    tp.order = p->order;
+    tp.limiter = p->limiter;
+    tp.gamma = p->gamma;
+    tp.R = p->R;
+    double lamy;
+    item_consts(*p, &tp.CV, &tp.lam, &lamy);
+    tp.alpha = (float)p->mc_alpha;
+    {
+        int ex;
+        tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
+    }
+    tp.steps = (int)nsteps;
+    tp.par = 0;
+    Chunk chunks[kStaticMaxChunks];
+    const int n = tp.n;
+    const int S = chunk_owned(tp.order, B);
+    int k = n <= MW ? 2 : (n + S - 1) / S;
+    if (k > n) k = n;
+    if (k > kStaticMaxChunks) {
+        fprintf(stderr, "shll_tube_run_static: %d chunks exceed the static limit %d\n", k, kStaticMaxChunks);
+        return SHLL_ERR_ARG;
+    }
+    for (int c = 0; c < k; c++) {
+        const int a = (int)((long)n * c / k), b = (int)((long)n * (c + 1) / k);
+        const int anc = c == 0 ? 0 : (c == k - 1 ? n - 1 : (a + b) / 2);
+        chunks[c] = {0, a, b, anc, c, c > 0 ? c - 1 : -1, c + 1 < k ? c + 1 : -1};
+    }
+    TubeP* d_tube = reinterpret_cast<TubeP*>(sc + kStaticTubeOff);
+    Chunk* d_chunks = reinterpret_cast<Chunk*>(sc + kStaticChunkOff);
+    int* d_flag = reinterpret_cast<int*>(sc + kStaticFlagOff);
+    cudaError_t e = cudaMemcpyAsync(d_tube, &tp, sizeof(tp), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_chunks, chunks, sizeof(Chunk) * k, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), s);  // the flag must start clear
+    if (e != cudaSuccess) {
+        fprintf(stderr, "shll_tube_run_static: descriptor upload failed: %s\n", cudaGetErrorString(e));
+        return SHLL_ERR_CUDA;
+    }
+    SweepArgs A;
+    A.tubes = d_tube;
+    A.chunks = d_chunks;
+    A.hi[0] = d_cons;
+    A.hi[1] = sc;  // the second state buffer
+    A.lo[0] = A.lo[1] = nullptr;
+    A.bsum[0] = reinterpret_cast<BSum*>(sc + kStaticBSumOff);
+    A.bsum[1] = A.bsum[0] + kStaticMaxChunks;
+    A.plane = n;
+    A.B = B;
+    A.flag = d_flag;
+    const long nsweeps = (nsteps + B - 1) / B;
+    shll_count_launches(nsweeps + 1);
+    for (long w = 0; w < nsweeps; w++) {
+        A.sweep = (int)w;
+        k_sweep1d<false><<<k, MT, 0, s>>>(A);
+    }
+    k_fixup1d<false><<<(k + 127) / 128, 128, 0, s>>>(A, k);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && (nsweeps & 1))  // the result ended in the scratch buffer: copy it back
+        e = cudaMemcpyAsync(d_cons, sc, (size_t)3 * n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "shll_tube_run_static: %s\n", cudaGetErrorString(e));
+        return SHLL_ERR_CUDA;
+    }
+    if (flag & SHLL_FLAG_BADARG) return SHLL_ERR_ARG;
+    if (flag & SHLL_FLAG_NONPOSITIVE) return SHLL_ERR_NUMERIC;
     return SHLL_OK;
 }
