@@ -1,19 +1,27 @@
 #!/usr/bin/env python
-"""Benchmark of the SHLL Euler hot path on one GB300 (or N replicas under torchrun).
+"""Benchmark of the SHLL Euler hot path on one GB300 (or N independent replicas under torchrun).
 
 Metric: cell-updates/s of the FP32-flux / FP64-accumulate solver (SHLL_PREC_MIXED_F64), next to
-the plain FP64 one-launch-per-step path, with the L1 error against the FP64 path and the
-fraction of the HBM roofline (48 algorithmic bytes per 1D cell-update: 3 FP64 conserved values
-read and written once).
+the plain FP64 path (one launch per time step), with the L1 error against FP64 and the fraction of
+the HBM roofline (algorithmic bytes per cell-update: 48 in 1D = 3 FP64 conserved values read and
+written once, 64 in 2D).
 
-Default workload (one "step" of this benchmark = one full run of it): 1D Sod shock tube,
-second-order SHLL as the x sweep of base-c/2nd_order_base_shll.c, 65536 cells on [0,1],
-diaphragm at 0.5, rho 10/1, T 1/1, gas at rest, gamma 1.4, R 1, CFL 0.25, to t = 0.2
-(104858 time steps); synthetic initial data generated on the host.
+Workloads (all inputs are seeded synthetic initial data generated on the host; gamma 1.4, R 1,
+kinetic CFL 0.25):
+  sod1d    (default) 1D Sod tube, second-order SHLL (the x sweep of base-c/2nd_order_base_shll.c),
+           65536 cells, diaphragm 0.5, rho 10/1, T 1/1, at rest, to t = 0.2 (104858 steps).
+  circle2d 2D first-order SHLL (base-c/base_shll_2d.c), 4096 x 4096, circular diaphragm r = 0.25
+           at (0.5, 0.5), rho 10 inside / 1 outside, T 1, at rest, 500 steps.
+  batch1d  4096 tubes, seed 0: cells log-uniform in [256, 16384], density ratio U(2,100), temperature
+           ratio U(0.5,2), diaphragm U(0.3,0.7); first order for the first 2048, second order after;
+           each to t = 0.2.
+  batch2d  256 first-order domains, seed 1: side uniform in {128, 256, 512, 1024}, radius U(0.1,0.35),
+           density ratio U(2,50), temperature ratio U(0.5,2), at rest, 400 steps each.
+One benchmark "step" is one full run of the workload.
 
---impl reference times the reference's CPU implementation of the same path on the host cores
-(the bit-exact CPU port of base-c in its published FP32 arithmetic: the reference's own sources
-are not present on the GPU host), on a bounded sample of the same tube.
+--impl reference times the reference's CPU implementation of the path on the host cores (the
+bit-exact CPU port of base-c in its published FP32 arithmetic, test infrastructure of this
+repository: the reference's own sources are not present on the GPU host), on a bounded sample.
 """
 import argparse
 import importlib.util
@@ -42,6 +50,13 @@ def load_pkg():
     sys.modules[name] = mod
     spec.loader.exec_module(mod)
     return mod
+
+
+def oracle_mod():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.lib()
+    return O
 
 
 def peaks():
@@ -89,22 +104,29 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(s[0]) for s in self.samples) if v is not None]
+        mx = [v for v in (num(s[1]) for s in self.samples) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def profile_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` recorded in profiles/*.md ('traffic_bytes_per_launch:')."""
+def profile_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` on `workload` from profiles/*.md
+    ('kernel: <name>', 'workload: <name>', 'traffic_bytes_per_launch: <bytes>')."""
     try:
         for fn in sorted(os.listdir(PROFILES)):
             if not fn.endswith(".md"):
                 continue
             txt = open(os.path.join(PROFILES, fn)).read()
-            if f"kernel: {kernel}" in txt:
+            if f"kernel: {kernel}\n" in txt and f"workload: {workload}\n" in txt:
                 for line in txt.splitlines():
                     if line.startswith("traffic_bytes_per_launch:"):
                         return float(line.split(":")[1])
@@ -113,15 +135,96 @@ def profile_traffic(kernel):
     return None
 
 
-def sod_params(shll, n, order, precision, **kw):
-    return shll.params(1, order, nx=n, precision=precision, t_end=0.2, **kw)
+# ---------------------------------------------------------------------------------------------
+# workloads
+
+
+def items_batch1d(shll, precision, count=4096, seed=0, fold=0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(256), math.log(16384)))))
+        ratio = float(rng.uniform(2, 100))
+        tr = float(rng.uniform(0.5, 2))
+        xd = float(rng.uniform(0.3, 0.7))
+        order = 1 if t < count // 2 else 2
+        out.append(shll.params(1, order, nx=n, precision=precision, t_end=0.2, fold_steps=fold, ic_x_d=xd,
+                               ic_rho_l=ratio, ic_T_l=tr, ic_rho_r=1.0, ic_T_r=1.0, ic_u_l=0.0, ic_u_r=0.0))
+    return out
+
+
+def items_batch2d(shll, precision, count=256, seed=1, fold=0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.choice([128, 256, 512, 1024]))
+        r = float(rng.uniform(0.1, 0.35))
+        ratio = float(rng.uniform(2, 50))
+        tr = float(rng.uniform(0.5, 2))
+        out.append(shll.params(2, 1, nx=n, ny=n, precision=precision, n_steps=400, fold_steps=fold,
+                               ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5, ic_cy=0.5, ic_radius=r, ic_rho_l=ratio,
+                               ic_T_l=tr, ic_rho_r=1.0, ic_T_r=1.0))
+    return out
+
+
+def params_single(shll, workload, precision, cells, order, fold):
+    if workload == "sod1d":
+        return shll.params(1, order, nx=cells, precision=precision, t_end=0.2, fold_steps=fold)
+    return shll.params(2, 1, nx=cells, ny=cells, precision=precision, n_steps=500, fold_steps=fold,
+                       ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5, ic_cy=0.5, ic_radius=0.25, ic_rho_l=10.0,
+                       ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0)
+
+
+def describe(workload, cells, order):
+    return {
+        "sod1d": f"1D Sod shock tube, {'second' if order == 2 else 'first'}-order SHLL, {cells} cells, rho 10/1, "
+                 f"T 1/1, t=0.2",
+        "circle2d": f"2D first-order SHLL, {cells}x{cells}, circular diaphragm r=0.25, rho 10/1, T 1, 500 steps",
+        "batch1d": "4096 independent 1D tubes (seed 0), 256..16384 cells log-uniform, half first / half second "
+                   "order, each to t=0.2",
+        "batch2d": "256 independent 2D first-order domains (seed 1), 128^2..1024^2, circular diaphragms, 400 steps",
+    }[workload]
+
+
+class Problem:
+    """One workload instance on the GPU: single context or batch, with reset + timed run."""
+
+    def __init__(self, shll, workload, precision, cells, order, fold, stream):
+        self.shll, self.workload, self.stream = shll, workload, stream
+        self.batch = workload.startswith("batch")
+        self.dim = 2 if workload in ("circle2d", "batch2d") else 1
+        if self.batch:
+            gen = items_batch1d if workload == "batch1d" else items_batch2d
+            self.items = gen(shll, precision, fold=fold)
+            self.cu = sum(p.nx * (p.ny if p.dim == 2 else 1) * shll.steps_for(p) for p in self.items)
+        else:
+            self.p = params_single(shll, workload, precision, cells, order, fold)
+            self.cu = self.p.nx * (self.p.ny if self.p.dim == 2 else 1) * shll.steps_for(self.p)
+        self.obj = None
+
+    def reset(self):
+        """Brings the initial state onto the device (untimed)."""
+        if self.obj is not None:
+            self.obj.close()
+        if self.batch:
+            self.obj = self.shll.Batch(self.items)
+        else:
+            self.obj = self.shll.Context(self.p)
+            self.obj.init_state()
+        self.obj.set_stream(self.stream.cuda_stream)
+
+    def run(self):
+        self.obj.run()
+
+    def result(self):
+        if self.batch:
+            return [self.obj.primitives(i) for i in range(len(self.items))]
+        return self.obj.primitives()
 
 
 def cpu_sample(n, order, steps, bits):
-    """Times the CPU port of the reference (bit-exact FP32/FP64 port of base-c) on a sample."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    O.lib()
+    """Times the CPU port of the reference (bit-exact to base-c) on all n cells x `steps` steps."""
+    O = oracle_mod()
     cfg = O.make_cfg(order=order, nx=n, real_bits=bits, n_steps=steps)
     prim = O.ic_sod(n)
     t0 = time.perf_counter()
@@ -130,8 +233,36 @@ def cpu_sample(n, order, steps, bits):
     return n * steps / dt, dt
 
 
-def l2_flush(torch, buf):
-    buf.add_(1.0)
+def cpu_sample_2d(n, steps, bits):
+    O = oracle_mod()
+    cfg = O.make_cfg(dim=2, order=1, nx=n, ny=n, real_bits=bits, n_steps=steps)
+    prim = O.ic_circle2d(n, n, r=0.25)
+    t0 = time.perf_counter()
+    O.run(cfg, prim)
+    dt = time.perf_counter() - t0
+    return n * n * steps / dt, dt
+
+
+def reference_arm(args, workload, W):
+    """CPU reference timing (rank 0 only)."""
+    vals = []
+    for i in range(W + args.steps):
+        if workload in ("sod1d", "batch1d"):
+            n = args.cells if workload == "sod1d" else 4096
+            order = args.order if workload == "sod1d" else 2
+            steps = max(50, int(3.0e8 / n))
+            v, dt = cpu_sample(n, order, steps, 32)
+            sample = f"{n} cells x {steps} time steps per step, FP32 as published, 1 thread"
+        else:
+            n = 512
+            steps = max(20, int(2.0e8 / (n * n)))
+            v, dt = cpu_sample_2d(n, steps, 32)
+            sample = f"{n}x{n} cells x {steps} time steps per step, FP32 as published, 1 thread"
+        if i >= W:
+            vals.append((v, dt))
+    value = sum(v for v, _ in vals) / len(vals)
+    ms = 1000 * sum(dt for _, dt in vals) / len(vals)
+    return value, ms, sample
 
 
 def main():
@@ -140,39 +271,33 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cells", type=int, default=65536)
+    ap.add_argument("--workload", default="sod1d", choices=["sod1d", "circle2d", "batch1d", "batch2d"])
+    ap.add_argument("--cells", type=int, default=0, help="cells (1D) or side (2D); default per workload")
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--fold", type=int, default=0, help="fold interval of the mixed path (0 = library default)")
     ap.add_argument("--precision", default="mixed_f64")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison runs and CPU baseline")
     args = ap.parse_args()
-    W = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    workload = args.workload
+    if args.cells == 0:
+        args.cells = {"sod1d": 65536, "circle2d": 4096}.get(workload, 0)
+    W = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    n, order = args.cells, args.order
-    steps_per_run = None
-    workload = (f"1D Sod shock tube, {'second' if order == 2 else 'first'}-order SHLL, {n} cells, "
-                f"rho 10/1, T 1/1, t=0.2")
+    desc = describe(workload, args.cells, args.order)
+    config = {"workload": desc, "name": workload, "cells": args.cells or None,
+              "order": args.order if workload == "sod1d" else None}
 
     if args.impl == "reference":
         if rank != 0:
             return
-        # each step: a bounded sample of the same tube (all its cells, a slice of its time steps)
-        sample_steps = max(50, int(3.0e8 / n))
-        vals = []
-        for i in range(W + args.steps):
-            v, dt = cpu_sample(n, order, sample_steps, 32)
-            if i >= W:
-                vals.append((v, dt))
-        value = sum(v for v, _ in vals) / len(vals)
-        ms = 1000 * sum(dt for _, dt in vals) / len(vals)
-        sample = f"{n} cells x {sample_steps} of the run's time steps per step, FP32 as published, 1 thread"
+        value, ms, sample = reference_arm(args, workload, args.warmup)
         print(json.dumps({
             "impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": W, "ms_per_step": ms,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": workload, "cells": n, "order": order},
+            "data": "synthetic", "config": config,
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
@@ -186,122 +311,87 @@ def main():
         dist.init_process_group("nccl")
     shll = load_pkg()
     stream = torch.cuda.Stream()
-    p = sod_params(shll, n, order, args.precision, fold_steps=args.fold)
-    steps_per_run = shll.steps_for(p)
-    cu_per_run = steps_per_run * n
-    ctx = shll.Context(p)
-    ctx.set_stream(stream.cuda_stream)
-    ctx.init_state()
-    ctx.checkpoint()
+    prob = Problem(shll, workload, args.precision, args.cells, args.order, args.fold, stream)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     for _ in range(W):
-        ctx.restore()
-        ctx.run()
+        prob.reset()
+        prob.run()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     l0 = shll.kernel_launches()
+    launches = 0
     times = []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
+            prob.reset()
             with torch.cuda.stream(stream):
-                l2_flush(torch, flush)
-            ctx.restore()
+                flush.add_(1.0)
+            torch.cuda.synchronize()
+            la = shll.kernel_launches()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            ctx.run()
+            prob.run()
             e1.record(stream)
             e1.synchronize()
+            launches += shll.kernel_launches() - la
             times.append(e0.elapsed_time(e1) / 1000.0)
     torch.cuda.synchronize()
-    launches = shll.kernel_launches() - l0
     t_total = sum(times)
     if dist:
         t = torch.tensor([t_total], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_total = float(t.item())
         dist.barrier()
-    value = world * cu_per_run * args.steps / t_total
+    value = world * prob.cu * args.steps / t_total
     ms_per_step = 1000 * t_total / args.steps
-    mixed_out = ctx.primitives()
+    mixed_out = prob.result()
 
-    # roofline of the dominant kernel (the sweep kernel: fold_steps time steps per launch)
-    fold = args.fold if args.fold > 0 else 16
-    fold = min(fold, 32)
-    sweeps = math.ceil(steps_per_run / fold)
-    bytes_per_launch = 48.0 * n * fold
-    avg_launch = t_total / (args.steps * sweeps)  # upper bound: includes launch gaps
+    # roofline of the dominant kernel: algorithmic bytes / (timed region / its launches)
     hbm, peak_kind = peaks()
+    bytes_per_cu = 64.0 if prob.dim == 2 else 48.0
+    kernel = "k_step2d" if prob.dim == 2 else "k_sweep1d"
+    main_launches = max(1, launches - args.steps)  # minus the one fix-up launch per run
+    avg_launch = t_total / main_launches
+    bytes_per_launch = bytes_per_cu * prob.cu * args.steps / main_launches
     achieved = bytes_per_launch / avg_launch / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": profile_traffic("k_sweep1d"), "peak_kind": peak_kind,
-                "kernel": "k_sweep1d", "algorithmic_bytes_per_launch": bytes_per_launch,
-                "launch_duration_s": avg_launch}
+                "traffic": profile_traffic(kernel, workload), "peak_kind": peak_kind, "kernel": kernel,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "launch_duration_s": avg_launch,
+                "note": "launch duration = CUDA-event time of the timed runs / launches (includes gaps)"}
 
-    # end to end through the C-ABI with host buffers: upload primitives, run, download
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    x = np.arange(n)
-    rho = np.where(x < 0.5 * n, 10.0, 1.0)
-    u = np.zeros(n)
-    T = np.ones(n)
-    pe = sod_params(shll, n, order, args.precision, fold_steps=args.fold, ic_kind=shll.IC_USER)
-    ectx = shll.Context(pe)
-    ectx.set_primitives(rho, u, T)
-    ectx.run()  # warm
-    torch.cuda.synchronize()
+    # end to end through the C-ABI with host buffers: upload the initial state, run, download
     e_times = []
-    for _ in range(args.steps):
+    h2d = d2h = 0
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ectx.set_primitives(rho, u, T)
-        ectx.run()
-        out = ectx.primitives()
+        prob.reset()
+        prob.run()
+        out = prob.result()
+        torch.cuda.synchronize()
         e_times.append(time.perf_counter() - t0)
-    e2e_value = world * cu_per_run * args.steps / sum(e_times)
-    ectx.close()
+    nv = 4 if prob.dim == 2 else 3
+    plist = prob.items if prob.batch else [prob.p]
+    cells_total = sum(p.nx * (p.ny if p.dim == 2 else 1) for p in plist)
+    h2d = d2h = nv * 8 * cells_total  # primitives up (or descriptors expanded on the host), primitives down
+    e2e_value = world * prob.cu * len(e_times) / sum(e_times)
 
     extras = {}
     if not args.no_extras and rank == 0:
-        # plain FP64 path, one launch per step (bit-exact to the FP64 reference): throughput + L1
-        pf = sod_params(shll, n, order, "f64_exact")
-        fctx = shll.Context(pf)
-        fctx.set_stream(stream.cuda_stream)
-        fctx.init_state()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        fctx.run()
-        e1.record(stream)
-        e1.synchronize()
-        t64 = e0.elapsed_time(e1) / 1000.0
-        f64_out = fctx.primitives()
-        fctx.close()
-        l1 = np.mean(np.abs(mixed_out - f64_out), axis=1)
-        import oracle as O
-        O.lib()
-        ex = O.riemann_exact(n, steps_per_run * (0.125 / n))
-        extras = {
-            "fp64_plain": {"value": cu_per_run / t64, "unit": "cell-updates/s", "schedule": "one launch per step",
-                           "precision": "f64_exact"},
-            "speedup_vs_fp64_plain": (cu_per_run / (t_total / args.steps)) / (cu_per_run / t64),
-            "l1_vs_fp64": {"rho": l1[0], "u": l1[1], "T": l1[2]},
-            "l1_rho_vs_exact_riemann": {"mixed": float(np.mean(np.abs(mixed_out[0] - ex[0]))),
-                                        "fp64": float(np.mean(np.abs(f64_out[0] - ex[0])))},
-        }
-        cpu_v, cpu_dt = cpu_sample(n, order, max(50, int(3.0e8 / n)), 32)
-        extras["cpu_baseline"] = {"value": cpu_v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
-                                  "sample": f"{n} cells x {max(50, int(3.0e8 / n))} time steps, FP32 as "
-                                            f"published, {cpu_dt:.1f} s"}
+        extras = fp64_comparison(shll, torch, stream, prob, args, mixed_out, t_total)
     if rank == 0:
         line = {
             "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32-flux+f64-acc", "data": "synthetic",
-            "config": {"workload": workload, "cells": n, "order": order, "time_steps_per_run": steps_per_run,
-                       "precision": args.precision, "fold_steps": fold, "parallelism": f"replicas{world}",
-                       "l2": "flushed between runs (256 MB write)"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64"
+            else args.precision, "data": "synthetic",
+            "config": dict(config, cell_updates_per_run=prob.cu, precision=args.precision,
+                           fold_steps=args.fold or 16, parallelism=f"replicas{world}",
+                           l2="flushed between runs (256 MB write)"),
             "roofline": roofline,
-            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 3 * n * 8,
-                    "d2h_bytes_per_step": 3 * n * 8},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }
@@ -309,6 +399,85 @@ def main():
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def cpu_baseline(workload, args):
+    """The CPU port of the reference timed on a bounded sample of the workload, 1 thread."""
+    if workload in ("sod1d", "batch1d"):
+        n = args.cells if workload == "sod1d" else 4096
+        order = args.order if workload == "sod1d" else 2
+        steps = max(50, int(3.0e8 / n))
+        v, dt = cpu_sample(n, order, steps, 32)
+        sample = f"{n} cells x {steps} time steps ({'order ' + str(order)}), FP32 as published, {dt:.1f} s"
+    else:
+        n = 512
+        steps = max(20, int(2.0e8 / (n * n)))
+        v, dt = cpu_sample_2d(n, steps, 32)
+        sample = f"{n}x{n} cells x {steps} time steps, FP32 as published, {dt:.1f} s"
+    return {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port", "sample": sample}
+
+
+def fp64_comparison(shll, torch, stream, prob, args, mixed_out, t_mixed):
+    """Plain FP64 path (one launch per step) on the same workload (or a seeded subsample for the
+    batches): throughput, L1 of the mixed result against it, CPU baseline."""
+    out = {}
+    if prob.batch:
+        sub = 16 if prob.workload == "batch1d" else 8
+        gen = items_batch1d if prob.workload == "batch1d" else items_batch2d
+        items64 = gen(shll, "f64")[::sub]
+        idx = list(range(0, len(prob.items), sub))
+        b = shll.Batch(items64)
+        b.set_stream(stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run()
+        e1.record(stream)
+        e1.synchronize()
+        t64 = e0.elapsed_time(e1) / 1000.0
+        cu64 = sum(p.nx * (p.ny if p.dim == 2 else 1) * shll.steps_for(p) for p in items64)
+        l1 = np.zeros(4 if prob.dim == 2 else 3)
+        worst = 0.0
+        for j, i in enumerate(idx):
+            e = np.mean(np.abs(mixed_out[i] - b.primitives(j)), axis=1)
+            l1 += e / len(idx)
+            worst = max(worst, float(e[0]))
+        b.close()
+        out["fp64_plain"] = {"value": cu64 / t64, "unit": "cell-updates/s", "schedule": "one launch per step",
+                             "precision": "f64", "sample": f"every {sub}th item ({len(items64)} items)"}
+        out["speedup_vs_fp64_plain"] = (prob.cu / (t_mixed / args.steps)) / (cu64 / t64)
+        names = ["rho", "u", "v", "T"] if prob.dim == 2 else ["rho", "u", "T"]
+        out["l1_vs_fp64"] = dict(zip(names, [float(x) for x in l1]), rho_worst_item=worst)
+        out["cpu_baseline"] = cpu_baseline(prob.workload, args)
+        return out
+    prec64 = "f64_exact" if prob.workload == "sod1d" else "f64"
+    p64 = params_single(shll, prob.workload, prec64, args.cells, args.order, 0)
+    ctx = shll.Context(p64)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.init_state()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.run()
+    e1.record(stream)
+    e1.synchronize()
+    t64 = e0.elapsed_time(e1) / 1000.0
+    f64_out = ctx.primitives()
+    ctx.close()
+    l1 = np.mean(np.abs(mixed_out - f64_out), axis=1)
+    names = ["rho", "u", "v", "T"] if prob.dim == 2 else ["rho", "u", "T"]
+    out["fp64_plain"] = {"value": prob.cu / t64, "unit": "cell-updates/s", "schedule": "one launch per step",
+                         "precision": prec64}
+    out["speedup_vs_fp64_plain"] = (prob.cu / (t_mixed / args.steps)) / (prob.cu / t64)
+    out["l1_vs_fp64"] = dict(zip(names, [float(x) for x in l1]))
+    if prob.workload == "sod1d":
+        O = oracle_mod()
+        n = args.cells
+        ex = O.riemann_exact(n, shll.steps_for(prob.p) * (0.125 / n))
+        out["l1_rho_vs_exact_riemann"] = {"mixed": float(np.mean(np.abs(mixed_out[0] - ex[0]))),
+                                          "fp64": float(np.mean(np.abs(f64_out[0] - ex[0])))}
+    out["cpu_baseline"] = cpu_baseline(prob.workload, args)
+    return out
 
 
 if __name__ == "__main__":

@@ -161,11 +161,14 @@ int shll_save_results(shll_ctx* ctx, const char* path);
 
 /* ---- batches of independent tubes / domains ---- */
 typedef struct shll_batch shll_batch;
-/* items: count parameter sets (all dim 1, or all dim 2, any sizes/orders/initial data);
- * precision must be a MIXED mode or F64 for every item. */
+/* items: count parameter sets (all dim 1, or all dim 2, any sizes/orders/initial data), all
+ * with one precision: SHLL_PREC_F64 (the plain FP64 arithmetic, one launch per time step over
+ * every item) or a MIXED mode (the sweep engine in 1D; first order only in 2D). */
 int shll_batch_create(const shll_params* items, int count, shll_batch** out);
 /* Runs every item to its own end (its own DT and step count). */
 int shll_batch_run(shll_batch* b);
+/* Runs the batch's work on a cudaStream_t (NULL = its own stream). */
+int shll_batch_set_stream(shll_batch* b, void* cuda_stream);
 int shll_batch_get_primitives(shll_batch* b, int item, double* rho, double* u, double* v,
                               double* T);
 int shll_batch_totals(shll_batch* b, int item, double* out);

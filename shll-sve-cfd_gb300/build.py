@@ -25,8 +25,9 @@ UNITS = {
     "mixed1d.cu": ["-fmad=false"],
     "mixed2d.cu": ["-fmad=false"],
     "reduce.cu": [],
+    "plain_batch.cu": [],
 }
-HEADERS = ["shll_internal.h", "shll_plain.cuh", "mixed.h", "mixed_common.cuh"]
+HEADERS = ["shll_internal.h", "shll_plain.cuh", "mixed.h", "mixed_common.cuh", "plain_batch.h"]
 
 
 def _stale(target, deps):

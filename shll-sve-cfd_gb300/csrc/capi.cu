@@ -13,6 +13,7 @@
 
 #include "../../include/shll.h"
 #include "mixed.h"
+#include "plain_batch.h"
 #include "shll_internal.h"
 
 struct shll_ctx {
@@ -646,7 +647,8 @@ extern "C" double shll_ref_dt(void) { return g_ref ? g_ref->DT : 0.0; }
 
 // ---------------- batches ----------------
 struct shll_batch {
-    MixedState* m = nullptr;
+    MixedState* m = nullptr;     // mixed-precision items
+    PlainBatch* pb = nullptr;    // SHLL_PREC_F64 items (one launch per step)
     cudaStream_t stream = nullptr;
     int count = 0;
     bool loaded = false;
@@ -669,14 +671,26 @@ extern "C" int shll_batch_create(const shll_params* items, int count, shll_batch
     if (!b) return SHLL_ERR_NOMEM;
     b->count = count;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { delete b; return SHLL_ERR_CUDA; }
-    b->m = mixed_create_batch(items, count, b->stream, b->err, sizeof(b->err));
-    if (!b->m) {
-        fprintf(stderr, "shll_batch_create: %s\n", b->err);
-        cudaStreamDestroy(b->stream);
-        delete b;
-        return SHLL_ERR_NOMEM;
+    int rc;
+    if (items[0].precision == SHLL_PREC_F64) {
+        b->pb = plain_batch_create(items, count, b->stream, b->err, sizeof(b->err));
+        if (!b->pb) {
+            fprintf(stderr, "shll_batch_create: %s\n", b->err);
+            cudaStreamDestroy(b->stream);
+            delete b;
+            return SHLL_ERR_ARG;
+        }
+        rc = plain_batch_load(b->pb, b->err, sizeof(b->err));
+    } else {
+        b->m = mixed_create_batch(items, count, b->stream, b->err, sizeof(b->err));
+        if (!b->m) {
+            fprintf(stderr, "shll_batch_create: %s\n", b->err);
+            cudaStreamDestroy(b->stream);
+            delete b;
+            return SHLL_ERR_NOMEM;
+        }
+        rc = mixed_load_all(b->m, b->err, sizeof(b->err));
     }
-    int rc = mixed_load_all(b->m, b->err, sizeof(b->err));
     if (rc != SHLL_OK) { shll_batch_destroy(b); return rc; }
     b->loaded = true;
     *out = b;
@@ -685,32 +699,46 @@ extern "C" int shll_batch_create(const shll_params* items, int count, shll_batch
 
 extern "C" int shll_batch_run(shll_batch* b) {
     if (!b) return SHLL_ERR_ARG;
-    int rc = mixed_step(b->m, -1, b->err, sizeof(b->err));
+    int rc = b->pb ? plain_batch_run(b->pb, b->err, sizeof(b->err)) : mixed_step(b->m, -1, b->err, sizeof(b->err));
     if (rc != SHLL_OK) return rc;
-    int f = mixed_flags(b->m);
+    int f = b->pb ? plain_batch_flags(b->pb) : mixed_flags(b->m);
     if (f & SHLL_FLAG_TIMEOUT) { snprintf(b->err, sizeof(b->err), "a bounded device wait expired"); return SHLL_ERR_TIMEOUT; }
     if (f & SHLL_FLAG_BADARG) { snprintf(b->err, sizeof(b->err), "a kernel rejected its launch arguments"); return SHLL_ERR_ARG; }
     if (f & SHLL_FLAG_NONPOSITIVE) { snprintf(b->err, sizeof(b->err), "non-positive density/energy reached"); return SHLL_ERR_NUMERIC; }
     return SHLL_OK;
 }
 
+extern "C" int shll_batch_set_stream(shll_batch* b, void* stream) {
+    if (!b) return SHLL_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    if (b->m) mixed_set_stream(b->m, s);
+    if (b->pb) plain_batch_set_stream(b->pb, s);
+    return SHLL_OK;
+}
+
 extern "C" int shll_batch_get_primitives(shll_batch* b, int item, double* rho, double* u, double* v, double* T) {
     if (!b) return SHLL_ERR_ARG;
+    if (b->pb) return plain_batch_item_primitives(b->pb, item, rho, u, v, T, b->err, sizeof(b->err));
     return mixed_item_primitives(b->m, item, rho, u, v, T, b->err, sizeof(b->err));
 }
 
 extern "C" int shll_batch_totals(shll_batch* b, int item, double* out) {
     if (!b || !out) return SHLL_ERR_ARG;
+    if (b->pb) return plain_batch_item_totals(b->pb, item, out, b->err, sizeof(b->err));
     return mixed_item_totals(b->m, item, out, b->err, sizeof(b->err));
 }
 
-extern "C" long shll_batch_cell_updates(const shll_batch* b) { return b ? mixed_cell_updates(b->m) : -1; }
+extern "C" long shll_batch_cell_updates(const shll_batch* b) {
+    if (!b) return -1;
+    return b->pb ? plain_batch_cell_updates(b->pb) : mixed_cell_updates(b->m);
+}
 extern "C" const char* shll_batch_last_error(const shll_batch* b) { return b ? b->err : "no batch"; }
 
 extern "C" void shll_batch_destroy(shll_batch* b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    mixed_destroy(b->m);
+    if (b->m) mixed_destroy(b->m);
+    if (b->pb) plain_batch_destroy(b->pb);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }

@@ -547,7 +547,12 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
     }
     if (m->dim == 2) {
         m->B = fold;
-        if (!mixed2d_attach(m, err, len)) { delete m; return nullptr; }
+        if (cudaMalloc(&m->d_flag, sizeof(int)) != cudaSuccess || cudaMemset(m->d_flag, 0, sizeof(int)) != cudaSuccess) {
+            snprintf(err, len, "cudaMalloc of the error flag failed");
+            mixed_destroy(m);
+            return nullptr;
+        }
+        if (!mixed2d_attach(m, err, len)) { mixed_destroy(m); return nullptr; }
         return m;
     }
     // sweep length: the fold interval, capped so that a chunk keeps at least half its window
@@ -694,11 +699,12 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
         return SHLL_ERR_CUDA;
     }
     const long nsweeps = (maxsteps + m->B - 1) / m->B;
-    std::vector<int> active(nsweeps, 0);  // chunks whose tube still has sweep k
-    for (const Chunk& c : order) {
-        long sw = (m->tubes[c.tube].steps + m->B - 1) / m->B;
-        for (long k = 0; k < sw; k++) active[k]++;
-    }
+    // active[k] = chunks whose tube still has sweep k (suffix sum of a histogram of sweep counts)
+    std::vector<int> active(nsweeps + 1, 0);
+    for (const Chunk& c : order) active[(m->tubes[c.tube].steps + m->B - 1) / m->B]++;
+    for (long k = nsweeps - 1; k >= 0; k--) active[k] += active[k + 1];
+    std::vector<int> launch(nsweeps);
+    for (long k = 0; k < nsweeps; k++) launch[k] = active[k + 1];
     SweepArgs A;
     A.tubes = m->d_tubes;
     A.chunks = m->d_chunks;
@@ -712,8 +718,9 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     shll_count_launches(nsweeps + 1);
     for (long k = 0; k < nsweeps; k++) {
         A.sweep = (int)k;
-        if (m->kahan) k_sweep1d<true><<<active[k], MT, 0, m->stream>>>(A);
-        else k_sweep1d<false><<<active[k], MT, 0, m->stream>>>(A);
+        if (launch[k] == 0) continue;
+        if (m->kahan) k_sweep1d<true><<<launch[k], MT, 0, m->stream>>>(A);
+        else k_sweep1d<false><<<launch[k], MT, 0, m->stream>>>(A);
     }
     const int nch = (int)order.size();
     if (m->kahan) k_fixup1d<true><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);

@@ -81,20 +81,21 @@ constexpr int T1 = 256;  // cells per block (1D)
 
 // One fused time step in 1D: P and split fluxes for the block's cells plus halo (in shared
 // memory), slopes (order 2), then the reference's per-cell update.  Uin/Uout: 3 planes of n.
+// Body of one 1D block: cells [b0, b0+T1) of a tube of n cells whose component k lives at
+// U[k*stride + c].
 template <typename REAL, int ORDER>
-__global__ void __launch_bounds__(T1) k_step1(const REAL* __restrict__ Uin, REAL* __restrict__ Uout, int n,
-                                              Gas<REAL> g, int* __restrict__ flag) {
+__device__ __forceinline__ void step1_block(const REAL* __restrict__ Uin, REAL* __restrict__ Uout, int n, long stride,
+                                            const Gas<REAL>& g, int* __restrict__ flag, int b0) {
     constexpr int H = ORDER;
     constexpr int W = T1 + 2 * H;
     __shared__ REAL sfp[3][W], sfm[3][W];
     __shared__ REAL sdp[3][ORDER == 2 ? T1 + 2 : 1], sdm[3][ORDER == 2 ? T1 + 2 : 1];
-    const int b0 = blockIdx.x * T1;
     int bad = 0;
     for (int t = threadIdx.x; t < W; t += T1) {
         int c = b0 - H + t;
         REAL fp[3] = {0, 0, 0}, fm[3] = {0, 0, 0};
         if (c >= 0 && c < n) {
-            REAL u0 = Uin[c], u1 = Uin[n + c], u2 = Uin[2 * n + c], p1, p2, a;
+            REAL u0 = Uin[c], u1 = Uin[stride + c], u2 = Uin[2 * stride + c], p1, p2, a;
             prim1(g, u0, u1, u2, p1, p2, a);
             flux1(g, u0, u1, u2, p1, p2, a, fp, fm);
             bad |= !(u0 > (REAL)0) || !(p2 > (REAL)0);
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(T1) k_step1(const REAL* __restrict__ Uin, REAL
     const int s = threadIdx.x + H;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        REAL fp = sfp[k][s], fm = sfm[k][s], L, Rr, u = Uin[k * n + i];
+        REAL fp = sfp[k][s], fm = sfm[k][s], L, Rr, u = Uin[k * stride + i];
         if (ORDER == 1) {
             const REAL sg = (k == 1) ? (REAL)1 : (REAL)-1;  // reflective wall (base_shll.c:93-110)
             if (i == 0) { L = sg * fm; Rr = sfm[k][s + 1]; }
@@ -140,8 +141,14 @@ __global__ void __launch_bounds__(T1) k_step1(const REAL* __restrict__ Uin, REAL
             u = u - g.DT_ON_DX * (fp - fm + Rr - L);
             u = (REAL)(D(u) - 0.5 * D(g.DT_ON_DX) * D(sdp[k][d] + sdm[k][d] - Rdf - Ldf));
         }
-        Uout[k * n + i] = u;
+        Uout[k * stride + i] = u;
     }
+}
+
+template <typename REAL, int ORDER>
+__global__ void __launch_bounds__(T1) k_step1(const REAL* __restrict__ Uin, REAL* __restrict__ Uout, int n,
+                                              Gas<REAL> g, int* __restrict__ flag) {
+    step1_block<REAL, ORDER>(Uin, Uout, n, n, g, flag, blockIdx.x * T1);
 }
 
 // ---------------- 2D ----------------
@@ -194,17 +201,18 @@ constexpr size_t smem2() {
 
 // One fused 2D time step on a TI x TJ tile.  Shared memory holds fp, fm, hp, hm (4 components
 // each) for the tile plus an ORDER-wide halo, then (order 2) the x and y slopes.
+// Body of one 2D tile with origin (i0, j0) of an nx x ny domain whose component k lives at
+// U[k*stride + i*ny + j].
 template <typename REAL, int ORDER>
-__global__ void __launch_bounds__(TI * TJ) k_step2(const REAL* __restrict__ Uin, REAL* __restrict__ Uout, int nx,
-                                                   int ny, Gas<REAL> g, int* __restrict__ flag) {
+__device__ __forceinline__ void step2_tile(const REAL* __restrict__ Uin, REAL* __restrict__ Uout, int nx, int ny,
+                                           long stride, const Gas<REAL>& g, int* __restrict__ flag, int i0, int j0) {
     using TL = Tile2<ORDER>;
     constexpr int H = TL::H, WJ = TL::WJ, CELLS = TL::CELLS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     REAL* sf = reinterpret_cast<REAL*>(smem_raw);      // [16][CELLS]: fp0..3 fm0..3 hp0..3 hm0..3
     REAL* sd = sf + 16 * CELLS;                          // order 2 slopes
     constexpr int NXS = (TI + 2) * TJ, NYS = TI * (TJ + 2);
-    const int n = nx * ny;
-    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+    const long n = stride;
     const int tid = threadIdx.y * TJ + threadIdx.x;
     int bad = 0;
     for (int t = tid; t < CELLS; t += TI * TJ) {
@@ -298,6 +306,12 @@ __global__ void __launch_bounds__(TI * TJ) k_step2(const REAL* __restrict__ Uin,
         }
         Uout[k * n + c] = u;
     }
+}
+
+template <typename REAL, int ORDER>
+__global__ void __launch_bounds__(TI * TJ) k_step2(const REAL* __restrict__ Uin, REAL* __restrict__ Uout, int nx,
+                                                   int ny, Gas<REAL> g, int* __restrict__ flag) {
+    step2_tile<REAL, ORDER>(Uin, Uout, nx, ny, (long)nx * ny, g, flag, blockIdx.y * TI, blockIdx.x * TJ);
 }
 
 // ---------------- staged kernels (the reference's separate stages) ----------------

@@ -55,6 +55,7 @@ EXPORTS = [
     "shll_batch_destroy", "shll_ref_configure", "shll_ref_context", "Allocate_and_Init_Memory",
     "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P", "Update_U_from_F", "Save_Results",
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
+    "shll_batch_set_stream",
 ]
 
 
@@ -95,6 +96,7 @@ def lib():
         L.shll_save_results.argtypes = [vp, ctypes.c_char_p]
         L.shll_batch_create.argtypes = [P, ctypes.c_int, ctypes.POINTER(vp)]
         L.shll_batch_run.argtypes = [vp]
+        L.shll_batch_set_stream.argtypes = [vp, vp]
         L.shll_batch_get_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
         L.shll_batch_totals.argtypes = [vp, ctypes.c_int, dp]
         L.shll_batch_cell_updates.argtypes = [vp]
@@ -263,6 +265,9 @@ class Batch:
 
     def run(self):
         self._ck(lib().shll_batch_run(self.h), "batch_run")
+
+    def set_stream(self, stream_ptr):
+        self._ck(lib().shll_batch_set_stream(self.h, stream_ptr), "batch_set_stream")
 
     def primitives(self, i):
         p = self.items[i]

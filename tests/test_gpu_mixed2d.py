@@ -1,0 +1,87 @@
+"""GPU tests of the 2D mixed-precision engine (first order, reflective walls) against the FP64
+oracle (a restatement of base-c/base_shll_2d.c pinned bit for bit to the reference).
+
+Tolerances: L1(rho, u, v, T) <= 1e-6 against the FP64 oracle; mass and energy conserved to
+<= 1e-12 relative (reflective walls)."""
+import numpy as np
+import pytest
+
+from helpers import l1
+
+pytestmark = pytest.mark.gpu
+
+
+def run(shll, p):
+    ctx = shll.Context(p)
+    ctx.init_state()
+    t0 = ctx.totals()
+    steps = ctx.run()
+    out = ctx.primitives()
+    t1 = ctx.totals()
+    ctx.close()
+    return steps, out, t0, t1
+
+
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+@pytest.mark.parametrize("nx,ny", [(16, 32), (40, 70), (64, 64), (100, 37), (2, 5)])
+def test_box_vs_fp64_oracle(shll, oracle, prec, nx, ny):
+    cfg = oracle.make_cfg(dim=2, order=1, nx=nx, ny=ny, t_end=0.1)
+    steps, ref, _ = oracle.run(cfg, oracle.ic_ref_box2d(nx, ny))
+    s, out, t0, t1 = run(shll, shll.params(2, 1, nx=nx, ny=ny, precision=prec, t_end=0.1))
+    assert s == steps
+    err = l1(out, ref)
+    assert np.all(err <= 1e-6), err
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+    assert abs(t1[3] - t0[3]) / t0[3] <= 1e-12
+
+
+@pytest.mark.parametrize("n,steps", [(96, 200), (130, 60)])
+def test_circle_vs_fp64_oracle(shll, oracle, n, steps):
+    cfg = oracle.make_cfg(dim=2, order=1, nx=n, ny=n, n_steps=steps)
+    prim = oracle.ic_circle2d(n, n, r=0.25, rho_in=10.0, rho_out=1.0)
+    _, ref, _ = oracle.run(cfg, prim)
+    p = shll.params(2, 1, nx=n, ny=n, precision="mixed_f64", n_steps=steps, ic_kind=shll.IC_CIRCLE2D,
+                    ic_cx=0.5, ic_cy=0.5, ic_radius=0.25, ic_rho_l=10.0, ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0)
+    s, out, t0, t1 = run(shll, p)
+    assert s == steps
+    assert np.all(l1(out, ref) <= 1e-6)
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+
+
+def test_partial_steps(shll, oracle):
+    nx, ny = 48, 40
+    cfg = oracle.make_cfg(dim=2, order=1, nx=nx, ny=ny, n_steps=50)
+    _, ref, _ = oracle.run(cfg, oracle.ic_ref_box2d(nx, ny))
+    ctx = shll.Context(shll.params(2, 1, nx=nx, ny=ny, precision="mixed_f64", n_steps=50))
+    ctx.init_state()
+    ctx.step(1)
+    ctx.step(20)
+    ctx.run()
+    assert ctx.steps_taken == 50
+    assert np.all(l1(ctx.primitives(), ref) <= 1e-6)
+
+
+def test_batch_of_domains(shll, oracle):
+    rng = np.random.default_rng(5)
+    items, refs = [], []
+    for k in range(6):
+        n = int(rng.choice([20, 33, 64, 80]))
+        r = float(rng.uniform(0.1, 0.35))
+        rin = float(rng.uniform(2, 50))
+        tin = float(rng.uniform(0.5, 2))
+        steps = int(rng.integers(10, 60))
+        items.append(shll.params(2, 1, nx=n, ny=n, precision="mixed_f64", n_steps=steps,
+                                 ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5, ic_cy=0.5, ic_radius=r, ic_rho_l=rin,
+                                 ic_T_l=tin, ic_rho_r=1.0, ic_T_r=1.0))
+        cfg = oracle.make_cfg(dim=2, order=1, nx=n, ny=n, n_steps=steps)
+        refs.append(oracle.run(cfg, oracle.ic_circle2d(n, n, r=r, rho_in=rin, T_in=tin))[1])
+    b = shll.Batch(items)
+    b.run()
+    for k, p in enumerate(items):
+        assert np.all(l1(b.primitives(k), refs[k]) <= 1e-6), k
+
+
+def test_second_order_2d_mixed_is_refused(shll):
+    with pytest.raises(shll.ShllError) as e:
+        shll.Context(shll.params(2, 2, nx=32, ny=32, precision="mixed_f64"))
+    assert e.value.status == shll.ERR_NOMEM or e.value.status == shll.ERR_UNSUPPORTED

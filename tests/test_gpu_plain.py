@@ -217,3 +217,35 @@ def test_call_order_errors(shll):
     with pytest.raises(shll.ShllError) as e:
         ctx.set_primitives(np.zeros(16), np.zeros(16), np.ones(16))
     assert e.value.status == shll.ERR_ARG
+
+
+def test_plain_fp64_batch_1d_matches_oracle(shll, oracle):
+    # the one-launch-per-step FP64 schedule over many tubes of different sizes, orders and data
+    rng = np.random.default_rng(11)
+    items, refs = [], []
+    for k in range(10):
+        n = int(rng.integers(3, 700))
+        order = 1 + k % 2
+        xd, rl, tl = float(rng.uniform(0.3, 0.7)), float(rng.uniform(2, 100)), float(rng.uniform(0.5, 2))
+        items.append(shll.params(1, order, nx=n, precision="f64", ic_x_d=xd, ic_rho_l=rl, ic_T_l=tl))
+        cfg = oracle.make_cfg(order=order, nx=n)
+        refs.append(oracle.run(cfg, oracle.ic_sod(n, x_d=xd, rhoL=rl, TL=tl))[1])
+    b = shll.Batch(items)
+    b.run()
+    for k in range(len(items)):
+        assert max_rel_scaled(b.primitives(k), refs[k]) <= 1e-10, k
+    assert b.cell_updates == sum(p.nx * shll.steps_for(p) for p in items)
+
+
+def test_plain_fp64_batch_2d_matches_oracle(shll, oracle):
+    items, refs = [], []
+    for k, (n, r) in enumerate([(20, 0.2), (37, 0.3), (64, 0.15)]):
+        items.append(shll.params(2, 1, nx=n, ny=n, precision="f64", n_steps=40 + 10 * k, ic_kind=shll.IC_CIRCLE2D,
+                                 ic_cx=0.5, ic_cy=0.5, ic_radius=r, ic_rho_l=10.0, ic_T_l=1.0, ic_rho_r=1.0,
+                                 ic_T_r=1.0))
+        cfg = oracle.make_cfg(dim=2, order=1, nx=n, ny=n, n_steps=40 + 10 * k)
+        refs.append(oracle.run(cfg, oracle.ic_circle2d(n, n, r=r))[1])
+    b = shll.Batch(items)
+    b.run()
+    for k in range(len(items)):
+        assert max_rel_scaled(b.primitives(k), refs[k]) <= 1e-10, k
