@@ -172,6 +172,9 @@ int shll_batch_set_stream(shll_batch* b, void* cuda_stream);
 int shll_batch_get_primitives(shll_batch* b, int item, double* rho, double* u, double* v,
                               double* T);
 int shll_batch_totals(shll_batch* b, int item, double* out);
+/* SHLL_OK, or SHLL_ERR_NUMERIC if this item reached a non-positive or NaN density/energy (the
+ * other items are unaffected; shll_batch_run returns SHLL_ERR_NUMERIC if any item did). */
+int shll_batch_item_status(shll_batch* b, int item);
 long shll_batch_cell_updates(const shll_batch* b);
 const char* shll_batch_last_error(const shll_batch* b);
 void shll_batch_destroy(shll_batch* b);

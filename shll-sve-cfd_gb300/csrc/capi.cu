@@ -728,6 +728,12 @@ extern "C" int shll_batch_totals(shll_batch* b, int item, double* out) {
     return mixed_item_totals(b->m, item, out, b->err, sizeof(b->err));
 }
 
+extern "C" int shll_batch_item_status(shll_batch* b, int item) {
+    if (!b || item < 0 || item >= b->count) return SHLL_ERR_ARG;
+    const int f = b->pb ? plain_batch_item_flags(b->pb, item) : mixed_item_flags(b->m, item);
+    return (f & SHLL_FLAG_NONPOSITIVE) ? SHLL_ERR_NUMERIC : SHLL_OK;
+}
+
 extern "C" long shll_batch_cell_updates(const shll_batch* b) {
     if (!b) return -1;
     return b->pb ? plain_batch_cell_updates(b->pb) : mixed_cell_updates(b->m);

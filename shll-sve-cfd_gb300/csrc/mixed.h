@@ -32,6 +32,7 @@ int mixed_item_conserved(MixedState* m, int item, double* planes, char* err, siz
 long mixed_cell_updates(const MixedState* m);
 int mixed_checkpoint(MixedState* m, bool restore, char* err, size_t errlen);
 int mixed_flags(MixedState* m);
+int mixed_item_flags(MixedState* m, int item);
 
 // FP64 plane sums (reduce.cu)
 cudaError_t device_plane_sums(const void* planes, int real_bits, int nv, long n, double* out, cudaStream_t s);

@@ -112,6 +112,7 @@ struct SweepArgs {
     long plane;         // cells per plane (all tubes)
     int sweep, B;
     int* flag;
+    int* item_flags;    // per tube (may be null)
 };
 
 // correction owed to the first owned cell of the chunk with id `right` by its left neighbour
@@ -368,7 +369,10 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         const float eint = __fadd_rn(E, -__fmul_rn(0.5f, __fdividef(__fmul_rn(m, m), r)));
         bad |= !(r > 0.f) || !(eint > 0.f);
     }
-    if (bad) atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
+    if (bad) {
+        atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
+        if (A.item_flags) atomicOr(&A.item_flags[ch.tube], SHLL_FLAG_NONPOSITIVE);
+    }
 }
 
 template <bool KAHAN>
@@ -435,6 +439,7 @@ struct MixedState {
     Chunk* d_chunks = nullptr;
     std::vector<Chunk> chunks;         // sorted by the steps of their tube (descending)
     int* d_flag = nullptr;
+    int* d_item_flags = nullptr;       // per item
     BSum* bsum[2] = {nullptr, nullptr};  // boundary flux sums per chunk id, by sweep parity
     long cell_updates = 0;
     // device checkpoint (shll_checkpoint)
@@ -498,6 +503,11 @@ static int alloc_mixed(MixedState* m, char* err, size_t len) {
             return SHLL_ERR_NOMEM;
         }
     }
+    if (cudaMalloc(&m->d_item_flags, sizeof(int) * m->nitems) != cudaSuccess ||
+        cudaMemset(m->d_item_flags, 0, sizeof(int) * m->nitems) != cudaSuccess) {
+        snprintf(err, len, "cudaMalloc of item flags failed");
+        return SHLL_ERR_NOMEM;
+    }
     if (cudaMalloc(&m->d_tubes, sizeof(TubeP) * m->nitems) != cudaSuccess ||
         cudaMalloc(&m->d_flag, sizeof(int)) != cudaSuccess || cudaMemset(m->d_flag, 0, sizeof(int)) != cudaSuccess) {
         snprintf(err, len, "cudaMalloc of descriptors failed");
@@ -547,8 +557,10 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
     }
     if (m->dim == 2) {
         m->B = fold;
-        if (cudaMalloc(&m->d_flag, sizeof(int)) != cudaSuccess || cudaMemset(m->d_flag, 0, sizeof(int)) != cudaSuccess) {
-            snprintf(err, len, "cudaMalloc of the error flag failed");
+        if (cudaMalloc(&m->d_flag, sizeof(int)) != cudaSuccess || cudaMemset(m->d_flag, 0, sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&m->d_item_flags, sizeof(int) * count) != cudaSuccess ||
+            cudaMemset(m->d_item_flags, 0, sizeof(int) * count) != cudaSuccess) {
+            snprintf(err, len, "cudaMalloc of the error flags failed");
             mixed_destroy(m);
             return nullptr;
         }
@@ -607,6 +619,7 @@ void mixed_destroy(MixedState* m) {
     cudaFree(m->bsum[0]);
     cudaFree(m->bsum[1]);
     cudaFree(m->d_flag);
+    cudaFree(m->d_item_flags);
     delete m;
 }
 
@@ -663,12 +676,14 @@ static int load_tube(MixedState* m, int t, const double* prim, char* err, size_t
 
 int mixed_load(MixedState* m, const double* prim, char* err, size_t len) {
     cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+    cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
     if (m->dim == 2) return mixed2d_load(m, 0, prim, err, len);
     return load_tube(m, 0, prim, err, len);
 }
 
 int mixed_load_all(MixedState* m, char* err, size_t len) {
     cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+    cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
     for (int t = 0; t < m->nitems; t++) {
         const shll_params& p = m->items[t];
         std::vector<double> prim((size_t)(p.dim == 2 ? 4 : 3) * p.nx * (p.dim == 2 ? p.ny : 1));
@@ -714,6 +729,7 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     A.plane = m->plane;
     A.B = m->B;
     A.flag = m->d_flag;
+    A.item_flags = m->d_item_flags;
     A.sweep = 0;
     shll_count_launches(nsweeps + 1);
     for (long k = 0; k < nsweeps; k++) {
@@ -830,6 +846,15 @@ int mixed_totals(MixedState* m, double* out, char* err, size_t len) { return mix
 // accessors used by mixed2d.cu
 cudaStream_t mixed_stream(MixedState* m) { return m->stream; }
 int* mixed_flag_ptr(MixedState* m) { return m->d_flag; }
+int* mixed_item_flags_ptr(MixedState* m) { return m->d_item_flags; }
+
+int mixed_item_flags(MixedState* m, int item) {
+    if (item < 0 || item >= m->nitems || !m->d_item_flags) return 0;
+    int h = 0;
+    cudaMemcpyAsync(&h, m->d_item_flags + item, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+    cudaStreamSynchronize(m->stream);
+    return h;
+}
 const shll_params* mixed_items(MixedState* m, int* count) { *count = m->nitems; return m->items.data(); }
 void** mixed_d2_slot(MixedState* m) { return &m->d2; }
 int mixed_fold(MixedState* m) { return m->B; }
@@ -998,6 +1023,7 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.plane = n;
     A.B = B;
     A.flag = d_flag;
+    A.item_flags = nullptr;
     const long nsweeps = (nsteps + B - 1) / B;
     shll_count_launches(nsweeps + 1);
     for (long w = 0; w < nsweeps; w++) {

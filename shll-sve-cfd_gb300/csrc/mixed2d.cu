@@ -33,6 +33,7 @@
 
 cudaStream_t mixed_stream(MixedState* m);
 int* mixed_flag_ptr(MixedState* m);
+int* mixed_item_flags_ptr(MixedState* m);
 const shll_params* mixed_items(MixedState* m, int* count);
 void** mixed_d2_slot(MixedState* m);
 bool mixed_is_kahan(MixedState* m);
@@ -177,6 +178,7 @@ struct Args2 {
     long plane;
     int step;
     int* flag;
+    int* item_flags;
 };
 
 template <bool KAHAN>
@@ -370,7 +372,10 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
             if (k == 0) bad |= !(v > 0.0);
         }
     }
-    if (bad) atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
+    if (bad) {
+        atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
+        atomicOr(&A.item_flags[tile.dom], SHLL_FLAG_NONPOSITIVE);
+    }
 }
 
 // applies the last step's edge corrections to the edge cells (after the final step of a run)
@@ -556,6 +561,7 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
     A.ey[0] = d->ey[0]; A.ey[1] = d->ey[1];
     A.plane = d->plane;
     A.flag = mixed_flag_ptr(m);
+    A.item_flags = mixed_item_flags_ptr(m);
     const bool kahan = mixed_is_kahan(m);
     const int ntiles = (int)d->tiles.size();
     shll_count_launches(maxsteps + 1);

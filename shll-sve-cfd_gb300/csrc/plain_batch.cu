@@ -23,28 +23,29 @@ struct PItem {
 
 struct PBlk { int item, a, b; };  // 1D: first cell a; 2D: tile origin (a, b) = (i0, j0)
 
+// (flag points at the item's own flag word; the kernel ORs SHLL_FLAG_NONPOSITIVE into it)
 template <int ORDER>
 __global__ void __launch_bounds__(T1) k_batch1(const PItem* __restrict__ items, const PBlk* __restrict__ blks,
-                                               double* U0, double* U1, long plane, int step, int* flag) {
+                                               double* U0, double* U1, long plane, int step, int* flags) {
     const PBlk bk = blks[blockIdx.x];
     const PItem it = items[bk.item];
     if (step >= it.steps) return;
     const int inb = (it.par + step) & 1;
     const double* Uin = (inb ? U1 : U0) + it.base;
     double* Uout = (inb ? U0 : U1) + it.base;
-    step1_block<double, ORDER>(Uin, Uout, it.nx, plane, it.g, flag, bk.a);
+    step1_block<double, ORDER>(Uin, Uout, it.nx, plane, it.g, flags + bk.item, bk.a);
 }
 
 template <int ORDER>
 __global__ void __launch_bounds__(TI * TJ) k_batch2(const PItem* __restrict__ items, const PBlk* __restrict__ blks,
-                                                    double* U0, double* U1, long plane, int step, int* flag) {
+                                                    double* U0, double* U1, long plane, int step, int* flags) {
     const PBlk bk = blks[blockIdx.x];
     const PItem it = items[bk.item];
     if (step >= it.steps) return;
     const int inb = (it.par + step) & 1;
     const double* Uin = (inb ? U1 : U0) + it.base;
     double* Uout = (inb ? U0 : U1) + it.base;
-    step2_tile<double, ORDER>(Uin, Uout, it.nx, it.ny, plane, it.g, flag, bk.a, bk.b);
+    step2_tile<double, ORDER>(Uin, Uout, it.nx, it.ny, plane, it.g, flags + bk.item, bk.a, bk.b);
 }
 
 }  // namespace plain_batch_ns
@@ -103,7 +104,8 @@ PlainBatch* plain_batch_create(const shll_params* p, int count, cudaStream_t s, 
     bool ok = true;
     for (int k = 0; k < 2 && ok; k++) ok = cudaMalloc(&b->U[k], sizeof(double) * b->nv * off) == cudaSuccess;
     if (ok) ok = cudaMalloc(&b->d_items, sizeof(PItem) * count) == cudaSuccess;
-    if (ok) ok = cudaMalloc(&b->d_flag, sizeof(int)) == cudaSuccess && cudaMemset(b->d_flag, 0, sizeof(int)) == cudaSuccess;
+    if (ok) ok = cudaMalloc(&b->d_flag, sizeof(int) * count) == cudaSuccess &&
+                 cudaMemset(b->d_flag, 0, sizeof(int) * count) == cudaSuccess;  // one flag per item
     if (!ok) {
         snprintf(err, len, "plain batch: device allocation failed (%ld cells)", off);
         plain_batch_destroy(b);
@@ -228,8 +230,18 @@ int plain_batch_run(PlainBatch* b, char* err, size_t len) {
 }
 
 int plain_batch_flags(PlainBatch* b) {
+    std::vector<int> h(b->count);
+    cudaMemcpyAsync(h.data(), b->d_flag, sizeof(int) * b->count, cudaMemcpyDeviceToHost, b->stream);
+    cudaStreamSynchronize(b->stream);
+    int f = 0;
+    for (int v : h) f |= v;
+    return f;
+}
+
+int plain_batch_item_flags(PlainBatch* b, int t) {
+    if (t < 0 || t >= b->count) return 0;
     int h = 0;
-    cudaMemcpyAsync(&h, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->stream);
+    cudaMemcpyAsync(&h, b->d_flag + t, sizeof(int), cudaMemcpyDeviceToHost, b->stream);
     cudaStreamSynchronize(b->stream);
     return h;
 }

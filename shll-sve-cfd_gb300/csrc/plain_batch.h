@@ -13,6 +13,7 @@ void plain_batch_set_stream(PlainBatch* b, cudaStream_t s);
 int plain_batch_load(PlainBatch* b, char* err, size_t len);
 int plain_batch_run(PlainBatch* b, char* err, size_t len);
 int plain_batch_flags(PlainBatch* b);
+int plain_batch_item_flags(PlainBatch* b, int t);
 long plain_batch_cell_updates(const PlainBatch* b);
 int plain_batch_item_primitives(PlainBatch* b, int t, double* rho, double* u, double* v, double* T, char* err,
                                 size_t len);

@@ -55,7 +55,7 @@ EXPORTS = [
     "shll_batch_destroy", "shll_ref_configure", "shll_ref_context", "Allocate_and_Init_Memory",
     "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P", "Update_U_from_F", "Save_Results",
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
-    "shll_batch_set_stream",
+    "shll_batch_set_stream", "shll_batch_item_status",
 ]
 
 
@@ -97,6 +97,7 @@ def lib():
         L.shll_batch_create.argtypes = [P, ctypes.c_int, ctypes.POINTER(vp)]
         L.shll_batch_run.argtypes = [vp]
         L.shll_batch_set_stream.argtypes = [vp, vp]
+        L.shll_batch_item_status.argtypes = [vp, ctypes.c_int]
         L.shll_batch_get_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
         L.shll_batch_totals.argtypes = [vp, ctypes.c_int, dp]
         L.shll_batch_cell_updates.argtypes = [vp]
@@ -263,8 +264,17 @@ class Batch:
         if rc != OK:
             raise ShllError(rc, f"{what}: {lib().shll_batch_last_error(self.h).decode()}")
 
-    def run(self):
-        self._ck(lib().shll_batch_run(self.h), "batch_run")
+    def run(self, allow_numeric=False):
+        """Runs every item to its end.  allow_numeric: do not raise when some items reached a
+        non-positive/NaN state (check item_status)."""
+        rc = lib().shll_batch_run(self.h)
+        if rc == ERR_NUMERIC and allow_numeric:
+            return rc
+        self._ck(rc, "batch_run")
+        return rc
+
+    def item_status(self, i):
+        return lib().shll_batch_item_status(self.h, i)
 
     def set_stream(self, stream_ptr):
         self._ck(lib().shll_batch_set_stream(self.h, stream_ptr), "batch_set_stream")
