@@ -1,6 +1,7 @@
 // Mixed-precision 2D SHLL engine (first order, reflective walls): FP32 split fluxes in
-// perturbation form, state in FP64 (SHLL_PREC_MIXED_F64) or as an FP32 value + compensation
-// pair (SHLL_PREC_MIXED_KAHAN), one launch per time step over every tile of every domain.
+// perturbation form, state in FP64 (SHLL_PREC_MIXED_F64) or as an FP32 value + compensation pair
+// (SHLL_PREC_MIXED_KAHAN); one launch per time step over every tile of every domain, with the
+// stored state touched only once per fold window.
 //
 // The arithmetic is that of base-c/base_shll_2d.c:139-300 re-associated as interface fluxes:
 // cell (i,j) gains lam_x (F_{i-1/2} - F_{i+1/2}) + lam_y (H_{j-1/2} - H_{j+1/2}), with
@@ -8,17 +9,19 @@
 // components 0,2,3 of the split flux, y walls 0,1,3, so the wall flux is (0, 2 fm1, 0, 0) at
 // i = 0, (0, 2 fp1, 0, 0) at i = nx-1, (0, 0, 2 hm2, 0) at j = 0 and (0, 0, 2 hp2, 0) at j = ny-1).
 //
-//   * A tile (16 x 32 cells, one CTA) has one frame: the FP64 state of its centre cell at the start
-//     of the step and the split-flux coefficients derived from it.  The split fluxes of the tile's
-//     cells and of its one-cell halo are evaluated in FP32 as deviations from the frame
-//     (mixed_common.cuh), so rounding scales with |U - U*|.
+//   * Fold windows of fold_steps steps.  At a fold (k_fold2d) the stored state B absorbs the
+//     window's increments (FP64, or FP32-pair arithmetic), every tile (16 x 32 cells) gets a new
+//     frame (the state of its centre cell and the split-flux coefficients derived from it, kept
+//     in a per-tile table), and every cell stores C = B - U*(tile) rounded to FP32.
+//   * Each step (k_step2d) evaluates the split fluxes of the tile's cells and of its one-cell halo in
+//     FP32 as deviations from the tile's frame (own cells: C + P; halo cells: (B - U*) + P with the
+//     neighbour's B in FP64), so rounding scales with |U - U*|; it sums the cell's four interface
+//     terms exactly as an FP32 pair and adds them to the cell's increment pair P (TwoSum).
 //   * Inside a tile both cells of an interface add the same FP32 term lam*Delta with opposite
 //     signs.  Neighbouring tiles evaluate their shared interfaces in different frames; each tile
-//     records the full flux it applied on its edges, and at the next step the east/north tile's
-//     edge cells receive lam*(F_west/south tile - F_own), so the west/south value is the one that
-//     counts and mass, momentum and energy are conserved to the rounding of the state.
-//   * The four interface terms of a cell are summed exactly as an FP32 pair (TwoSum) and added to
-//     the state once per step (FP64 add, or FP32-pair add).
+//     records the full flux it applied on its edges, and the east/north tile's edge cells then
+//     receive lam*(F_west/south tile - F_own) (next step, or at the fold), so the west/south value
+//     is the one that counts: mass, momentum and energy are conserved to the rounding of B.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,24 +51,25 @@ constexpr int NT = TI * TJ;      // threads per CTA, one cell each
 constexpr int WI = TI + 2, WJ = TJ + 2;
 
 struct Dom2 {
-    long base;                // cell offset of the domain in the planes
+    int base;                 // cell offset of the domain in the planes
     int nx, ny, tiles_i, tiles_j;
-    long ex_base, ey_base;    // first edge entry of this domain in the x / y edge buffers
-    int steps, par;           // steps of the current run; buffer holding the state at its start
+    int tile_base;            // first tile of this domain in the tile / frame tables
+    int ex_base, ey_base;     // first edge entry of this domain in the x / y edge buffers
+    int steps;                // steps of the current run
     double gamma, R, CV, lamx, lamy;
+    float lxh, lxl, lyh, lyl; // lam_x, lam_y as FP32 pairs
 };
 
 struct TileD { int dom, ti, tj; };
 
-// one edge interface: the flux lam*F applied by the west/south tile (side 0) and by the
-// east/north tile (side 1), four components each
-struct Edge { double s[2][4]; };
+// one edge interface: the full flux lam*F applied by the west/south tile (side 0) and by the
+// east/north tile (side 1), four components each, as FP32 pairs (value, remainder)
+struct Edge { float r[2][4][2]; };
 
 struct Frame2 {
     double U[4], Fx[4], Fy[4];
     double fmS1, fpS1, hmS2, hpS2;   // wall split fluxes (reflective walls)
     AnchorCoef cx, cy;               // coefficients for the x and y split fluxes
-    float Uh[4], Ul[4];
 };
 
 __device__ void make_frame2(Frame2& f, const double U[4], const Dom2& d) {
@@ -81,8 +85,6 @@ __device__ void make_frame2(Frame2& f, const double U[4], const Dom2& d) {
     const double Z1y = 0.5 * (My + 1.0), Z2y = 0.5 * a * (1.0 - My * My), Z3y = 0.5 * (My - 1.0);
     for (int k = 0; k < 4; k++) {
         f.U[k] = U[k]; f.Fx[k] = Fx[k]; f.Fy[k] = Fy[k];
-        f.Uh[k] = (float)U[k];
-        f.Ul[k] = (float)(U[k] - (double)f.Uh[k]);
         f.cx.F[k] = (float)Fx[k]; f.cy.F[k] = (float)Fy[k];
         f.cx.Uf[k] = f.cy.Uf[k] = (float)U[k];
     }
@@ -168,39 +170,58 @@ __device__ __forceinline__ void dflux2(const AnchorCoef& cx, const AnchorCoef& c
     }
 }
 
+
+// Cell and plane offsets fit in 32 bits (the host refuses batches of more than 2^29 cells), so
+// the kernels index with int: 64-bit integer multiply-adds would run on the slow FP64 pipe.
 struct Args2 {
     const Dom2* doms;
     const TileD* tiles;
-    void* hi[2];
-    float* lo[2];
-    Edge* ex[2];     // x edge buffers by step parity
+    Frame2* frames;      // per tile, written by the fold
+    void* B;             // stored state: double[4][plane] or FP32 value planes (KAHAN)
+    float* Blo;          // FP32 compensation planes (KAHAN)
+    float* C;            // float[4][plane]: B - U*(tile) at the last fold
+    float* Ph[2];        // increment pairs since the last fold, by window-step parity
+    float* Pl[2];
+    Edge* ex[2];         // x / y edge buffers by step parity
     Edge* ey[2];
-    long plane;
-    int step;
+    int plane;
+    int step;            // global step of a k_step2d launch
+    int s0, win;         // fold window: first step and length (k_fold2d)
     int* flag;
     int* item_flags;
 };
 
 template <bool KAHAN>
-__device__ __forceinline__ double load2(const void* hi, const float* lo, long idx) {
-    if (KAHAN) return (double)static_cast<const float*>(hi)[idx] + (double)lo[idx];
-    return static_cast<const double*>(hi)[idx];
+__device__ __forceinline__ double loadB(const Args2& A, int idx) {
+    if (KAHAN) return (double)static_cast<const float*>(A.B)[idx] + (double)A.Blo[idx];
+    return static_cast<const double*>(A.B)[idx];
 }
 
-// boundary correction owed to cell (i, j) by the previous step (zero on the first step)
-__device__ __forceinline__ void cell_correction(const Args2& A, const Dom2& D, int i, int j, double c[4]) {
-    c[0] = c[1] = c[2] = c[3] = 0.0;
-    if (A.step == 0) return;
-    const int pp = (A.step - 1) & 1;
+// edge correction owed to cell (i, j) by the step whose edge buffers have parity pp:
+// lam*(F of the west/south tile - F of the cell's own tile) on its west / south edge line, as an
+// FP32 pair per component
+__device__ __forceinline__ void edge_correction(const Args2& A, const Dom2& D, int i, int j, int pp, float ch[4],
+                                                float cl[4]) {
+    for (int k = 0; k < 4; k++) { ch[k] = 0.f; cl[k] = 0.f; }
     if (i > 0 && i % TI == 0) {
-        const Edge& e = (pp ? A.ex[1] : A.ex[0])[D.ex_base + (long)(i / TI - 1) * D.ny + j];
-        for (int k = 0; k < 4; k++) c[k] += e.s[0][k] - e.s[1][k];
+        const Edge& e = (pp ? A.ex[1] : A.ex[0])[D.ex_base + (i / TI - 1) * D.ny + j];
+        for (int k = 0; k < 4; k++) {
+            two_sum_acc(ch[k], cl[k], e.r[0][k][0]);
+            two_sum_acc(ch[k], cl[k], -e.r[1][k][0]);
+            cl[k] = __fadd_rn(cl[k], __fadd_rn(e.r[0][k][1], -e.r[1][k][1]));
+        }
     }
     if (j > 0 && j % TJ == 0) {
-        const Edge& e = (pp ? A.ey[1] : A.ey[0])[D.ey_base + (long)(j / TJ - 1) * D.nx + i];
-        for (int k = 0; k < 4; k++) c[k] += e.s[0][k] - e.s[1][k];
+        const Edge& e = (pp ? A.ey[1] : A.ey[0])[D.ey_base + (j / TJ - 1) * D.nx + i];
+        for (int k = 0; k < 4; k++) {
+            two_sum_acc(ch[k], cl[k], e.r[0][k][0]);
+            two_sum_acc(ch[k], cl[k], -e.r[1][k][0]);
+            cl[k] = __fadd_rn(cl[k], __fadd_rn(e.r[0][k][1], -e.r[1][k][1]));
+        }
     }
 }
+
+__device__ __forceinline__ bool on_edge_line(int i, int j) { return (i > 0 && i % TI == 0) || (j > 0 && j % TJ == 0); }
 
 // (th, tl) = lam * x as an FP32 pair (exact when lam is an FP32 power of two)
 __device__ __forceinline__ void lam_mul(float lh, float ll, float x, float& th, float& tl) {
@@ -208,12 +229,80 @@ __device__ __forceinline__ void lam_mul(float lh, float ll, float x, float& th, 
     tl = __fadd_rn(__fmaf_rn(lh, x, -th), __fmul_rn(ll, x));
 }
 
+// ---- fold: B += P (+ the last edge corrections), new frames, C = B - U* ----
+template <bool KAHAN>
+__global__ void __launch_bounds__(NT) k_fold2d(Args2 A) {
+    __shared__ double sU[4];
+    __shared__ Frame2 fr;
+    const TileD tile = A.tiles[blockIdx.x];
+    const Dom2 D = A.doms[tile.dom];
+    const int wd = min(max(D.steps - A.s0, 0), A.win);  // steps this domain took in the window
+    if (A.win > 0 && wd == 0) return;                     // nothing changed since its last fold
+    const int tid = threadIdx.x;
+    const int i0 = tile.ti * TI, j0 = tile.tj * TJ;
+    const int hi_i = min(TI, D.nx - i0), hi_j = min(TJ, D.ny - j0);
+    const int li = tid / TJ, lj = tid % TJ;
+    const int i = i0 + li, j = j0 + lj;
+    const bool own = li < hi_i && lj < hi_j;
+    const int P = A.plane;
+    const int cell = D.base + i * D.ny + j;
+    double U[4] = {0, 0, 0, 0};
+    int bad = 0;
+    if (own) {
+        float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
+        if (wd > 0 && on_edge_line(i, j)) edge_correction(A, D, i, j, (A.s0 + wd - 1) & 1, ch, cl);
+        const float* ph = (wd & 1) ? A.Ph[1] : A.Ph[0];
+        const float* pl = (wd & 1) ? A.Pl[1] : A.Pl[0];
+        for (int k = 0; k < 4; k++) {
+            const int idx = k * P + cell;
+            if (KAHAN) {
+                float h = static_cast<float*>(A.B)[idx], l = A.Blo[idx];
+                if (wd > 0) {
+                    float oh, ol, qh = ph[idx], ql = pl[idx];
+                    two_sum_acc(qh, ql, ch[k]);
+                    ql = __fadd_rn(ql, cl[k]);
+                    ff_add(h, l, qh, ql, oh, ol);
+                    h = oh; l = ol;
+                    static_cast<float*>(A.B)[idx] = h;
+                    A.Blo[idx] = l;
+                }
+                U[k] = (double)h + (double)l;
+            } else {
+                double v = static_cast<double*>(A.B)[idx];
+                if (wd > 0) {
+                    v = v + ((double)ph[idx] + (double)pl[idx]) + ((double)ch[k] + (double)cl[k]);
+                    static_cast<double*>(A.B)[idx] = v;
+                }
+                U[k] = v;
+            }
+        }
+        bad = !(U[0] > 0.0) || !(U[3] > 0.0);
+        if (li == hi_i / 2 && lj == hi_j / 2)
+            for (int k = 0; k < 4; k++) sU[k] = U[k];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        make_frame2(fr, sU, D);
+        A.frames[D.tile_base + tile.ti * D.tiles_j + tile.tj] = fr;
+    }
+    __syncthreads();
+    if (own)
+        for (int k = 0; k < 4; k++) A.C[k * P + cell] = (float)(U[k] - fr.U[k]);
+    if (bad) {
+        atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
+        atomicOr(&A.item_flags[tile.dom], SHLL_FLAG_NONPOSITIVE);
+    }
+}
+
 struct Smem2 {
     Frame2 fr;
     float f[16][WI * WJ];   // dfp0..3, dfm0..3, dhp0..3, dhm0..3 of the window (tile + 1-cell halo)
     float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
+    float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
+    float dn[4][4][2];      // U*(neighbour) - U*(this) as pairs: [west, east, south, north][comp]
 };
 
+// ---- one time step of one tile ----
 template <bool KAHAN>
 __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
     __shared__ Smem2 S;
@@ -221,25 +310,22 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
     const Dom2 D = A.doms[tile.dom];
     if (A.step >= D.steps) return;
     const int tid = threadIdx.x;
+    const int kw = A.step - A.s0;                       // step within the fold window
     const int i0 = tile.ti * TI, j0 = tile.tj * TJ;
-    const int hi_i = min(TI, D.nx - i0), hi_j = min(TJ, D.ny - j0);  // tile extent
-    const int inb = (D.par + A.step) & 1;
-    const void* hin = inb ? A.hi[1] : A.hi[0];
-    const float* lin = inb ? A.lo[1] : A.lo[0];
-    void* hout = inb ? A.hi[0] : A.hi[1];
-    float* lout = inb ? A.lo[0] : A.lo[1];
-    const long P = A.plane;
-    const long base = D.base;
-    const float lxh = (float)D.lamx, lxl = (float)(D.lamx - (double)lxh);
-    const float lyh = (float)D.lamy, lyl = (float)(D.lamy - (double)lyh);
+    const int hi_i = min(TI, D.nx - i0), hi_j = min(TJ, D.ny - j0);
+    const int P = A.plane;
+    const int tb = D.tile_base + tile.ti * D.tiles_j + tile.tj;
+    const float* phi = (kw & 1) ? A.Ph[1] : A.Ph[0];    // increments so far (kw = 0: none)
+    const float* pli = (kw & 1) ? A.Pl[1] : A.Pl[0];
+    float* pho = (kw & 1) ? A.Ph[0] : A.Ph[1];
+    float* plo = (kw & 1) ? A.Pl[0] : A.Pl[1];
+    const int pp = (A.step - 1) & 1;                     // edge buffers of the previous step
+    const float lxh = D.lxh, lxl = D.lxl, lyh = D.lyh, lyl = D.lyl;
 
-    if (tid == 0) {
-        const int ia = i0 + hi_i / 2, ja = j0 + hi_j / 2;
-        double c[4], U[4];
-        cell_correction(A, D, ia, ja, c);
-        for (int k = 0; k < 4; k++) U[k] = load2<KAHAN>(hin, lin, k * P + base + (long)ia * D.ny + ja) + c[k];
-        make_frame2(S.fr, U, D);
-    }
+    // frame of this tile (written by the last fold)
+    static_assert(sizeof(Frame2) % 8 == 0, "frame copied as doubles");
+    for (int q = tid; q < (int)(sizeof(Frame2) / 8); q += NT)
+        reinterpret_cast<double*>(&S.fr)[q] = reinterpret_cast<const double*>(&A.frames[tb])[q];
     __syncthreads();
     if (tid < 16) {
         // constant wall terms: lam*(W_const - Fref) (west/south), lam*(Fref - W_const) (east/north)
@@ -251,16 +337,24 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
         else if (w == 2) v = k == 2 ? D.lamy * (2.0 * f.hmS2 - f.Fy[2]) : -D.lamy * f.Fy[k];
         else v = k == 2 ? D.lamy * (f.Fy[2] - 2.0 * f.hpS2) : D.lamy * f.Fy[k];
         split2(v, S.wc[w][k][0], S.wc[w][k][1]);
+        if (tid < 8) {
+            const int dir = tid / 4;
+            split2(dir == 0 ? D.lamx * f.Fx[k] : D.lamy * f.Fy[k], S.lf[dir][k][0], S.lf[dir][k][1]);
+        }
+        // frame of the neighbour tile w (0 west = ti-1, 1 east, 2 south = tj-1, 3 north)
+        const int ti = tile.ti + (w == 0 ? -1 : w == 1 ? 1 : 0), tj = tile.tj + (w == 2 ? -1 : w == 3 ? 1 : 0);
+        double dU = 0.0;
+        if (ti >= 0 && ti < D.tiles_i && tj >= 0 && tj < D.tiles_j)
+            dU = A.frames[D.tile_base + ti * D.tiles_j + tj].U[k] - f.U[k];
+        split2(dU, S.dn[w][k][0], S.dn[w][k][1]);
     }
-    // ---- split-flux deviations of the tile and its halo ----
-    const int li = tid / TJ, lj = tid % TJ;          // own cell, tile coordinates
+    __syncthreads();
+    const int li = tid / TJ, lj = tid % TJ;
     const int i = i0 + li, j = j0 + lj;
     const bool own = li < hi_i && lj < hi_j;
-    float Uh[4] = {0, 0, 0, 0}, Ul[4] = {0, 0, 0, 0};  // own state (KAHAN pair)
-    double Ud[4] = {0, 0, 0, 0};                      // own state (FP64)
-    // window slots: own cell, then halo slots handled by the first 2*(TI+TJ) threads
+    float Ph[4] = {0, 0, 0, 0}, Pl[4] = {0, 0, 0, 0};   // own increment pair
     for (int slot = 0; slot < 2; slot++) {
-        int wi, wj;   // window coordinates (0..WI-1, 0..WJ-1)
+        int wi, wj;   // window coordinates
         bool act;
         if (slot == 0) {
             wi = li + 1; wj = lj + 1; act = own;
@@ -276,26 +370,24 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
         float dfp[4] = {0, 0, 0, 0}, dfm[4] = {0, 0, 0, 0}, dhp[4] = {0, 0, 0, 0}, dhm[4] = {0, 0, 0, 0};
         if (act) {
             const int ci = i0 + wi - 1, cj = j0 + wj - 1;
-            const long idx = base + (long)ci * D.ny + cj;
-            double c[4];
-            cell_correction(A, D, ci, cj, c);
+            const int cell = D.base + ci * D.ny + cj;
+            // tile that owns the cell: this one (slot 0) or the west/east/south/north neighbour
+            const int nb = slot == 0 ? -1 : (wi == 0 ? 0 : wi == hi_i + 1 ? 1 : wj == 0 ? 2 : 3);
+            float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
+            if (kw > 0 && on_edge_line(ci, cj)) edge_correction(A, D, ci, cj, pp, ch, cl);
             float d[4];
             for (int k = 0; k < 4; k++) {
-                if (KAHAN) {
-                    float h = static_cast<const float*>(hin)[k * P + idx], l = lin[k * P + idx];
-                    if (c[k] != 0.0) {
-                        const double v = ((double)h + (double)l) + c[k];
-                        split2(v, h, l);
-                    }
-                    float dh, dl;
-                    ff_sub(h, l, S.fr.Uh[k], S.fr.Ul[k], dh, dl);
-                    d[k] = __fadd_rn(dh, dl);
-                    if (slot == 0) { Uh[k] = h; Ul[k] = l; }
-                } else {
-                    const double U = static_cast<const double*>(hin)[k * P + idx] + c[k];
-                    d[k] = (float)(U - S.fr.U[k]);
-                    if (slot == 0) Ud[k] = U;
-                }
+                const int idx = k * P + cell;
+                float h = 0.f, l = 0.f;
+                if (kw > 0) { h = phi[idx]; l = pli[idx]; }
+                two_sum_acc(h, l, ch[k]);   // the pending edge correction joins the increment pair
+                l = __fadd_rn(l, cl[k]);
+                if (slot == 0) { Ph[k] = h; Pl[k] = l; }
+                // deviation from this tile's frame: C (relative to the owner's frame) + the owner's
+                // frame offset + the increments
+                float base = A.C[idx];
+                if (nb >= 0) base = __fadd_rn(__fadd_rn(base, S.dn[nb][k][0]), S.dn[nb][k][1]);
+                d[k] = __fadd_rn(base, __fadd_rn(h, l));
             }
             dflux2(S.fr.cx, S.fr.cy, d, dfp, dfm, dhp, dhm);
         }
@@ -309,22 +401,22 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
     }
     __syncthreads();
     if (!own) return;
-    // ---- interface terms and the update of the own cell ----
+    // ---- interface terms and the increment of the own cell ----
     const int w = (li + 1) * WJ + (lj + 1);
     const int wW = w - WJ, wE = w + WJ, wS = w - 1, wN = w + 1;
     Edge* exo = A.step & 1 ? A.ex[1] : A.ex[0];
     Edge* eyo = A.step & 1 ? A.ey[1] : A.ey[0];
-    int bad = 0;
+    const int cell = D.base + i * D.ny + j;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const float fp = S.f[k][w], fm = S.f[4 + k][w], hp = S.f[8 + k][w], hm = S.f[12 + k][w];
-        float ah = 0.f, al = 0.f, th, tl;
+        float ah = Ph[k], al = Pl[k], th, tl;
         // x west
         if (i > 0) {
             const float Dw = __fadd_rn(S.f[k][wW], fm);
             lam_mul(lxh, lxl, Dw, th, tl);
             two_sum_acc(ah, al, th); al = __fadd_rn(al, tl);
-            if (li == 0) exo[D.ex_base + (long)(i / TI - 1) * D.ny + j].s[1][k] = D.lamx * S.fr.Fx[k] + ((double)th + (double)tl);
+            if (li == 0) { float* r = exo[D.ex_base + (i / TI - 1) * D.ny + j].r[1][k]; ff_add(S.lf[0][k][0], S.lf[0][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[0][k][0]); al = __fadd_rn(al, S.wc[0][k][1]);
             if (k == 1) { lam_mul(lxh, lxl, __fmul_rn(2.f, fm), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
@@ -334,7 +426,7 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
             const float De = __fadd_rn(fp, S.f[4 + k][wE]);
             lam_mul(lxh, lxl, De, th, tl);
             two_sum_acc(ah, al, -th); al = __fadd_rn(al, -tl);
-            if (li == hi_i - 1) exo[D.ex_base + (long)((i + 1) / TI - 1) * D.ny + j].s[0][k] = D.lamx * S.fr.Fx[k] + ((double)th + (double)tl);
+            if (li == hi_i - 1) { float* r = exo[D.ex_base + ((i + 1) / TI - 1) * D.ny + j].r[0][k]; ff_add(S.lf[0][k][0], S.lf[0][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[1][k][0]); al = __fadd_rn(al, S.wc[1][k][1]);
             if (k == 1) { lam_mul(lxh, lxl, -__fmul_rn(2.f, fp), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
@@ -344,7 +436,7 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
             const float Ds = __fadd_rn(S.f[8 + k][wS], hm);
             lam_mul(lyh, lyl, Ds, th, tl);
             two_sum_acc(ah, al, th); al = __fadd_rn(al, tl);
-            if (lj == 0) eyo[D.ey_base + (long)(j / TJ - 1) * D.nx + i].s[1][k] = D.lamy * S.fr.Fy[k] + ((double)th + (double)tl);
+            if (lj == 0) { float* r = eyo[D.ey_base + (j / TJ - 1) * D.nx + i].r[1][k]; ff_add(S.lf[1][k][0], S.lf[1][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[2][k][0]); al = __fadd_rn(al, S.wc[2][k][1]);
             if (k == 2) { lam_mul(lyh, lyl, __fmul_rn(2.f, hm), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
@@ -354,58 +446,13 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
             const float Dn = __fadd_rn(hp, S.f[12 + k][wN]);
             lam_mul(lyh, lyl, Dn, th, tl);
             two_sum_acc(ah, al, -th); al = __fadd_rn(al, -tl);
-            if (lj == hi_j - 1) eyo[D.ey_base + (long)((j + 1) / TJ - 1) * D.nx + i].s[0][k] = D.lamy * S.fr.Fy[k] + ((double)th + (double)tl);
+            if (lj == hi_j - 1) { float* r = eyo[D.ey_base + ((j + 1) / TJ - 1) * D.nx + i].r[0][k]; ff_add(S.lf[1][k][0], S.lf[1][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[3][k][0]); al = __fadd_rn(al, S.wc[3][k][1]);
             if (k == 2) { lam_mul(lyh, lyl, -__fmul_rn(2.f, hp), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
         }
-        const long idx = k * P + base + (long)i * D.ny + j;
-        if (KAHAN) {
-            float oh, ol;
-            ff_add(Uh[k], Ul[k], ah, al, oh, ol);
-            static_cast<float*>(hout)[idx] = oh;
-            lout[idx] = ol;
-            if (k == 0) bad |= !(oh > 0.f);
-        } else {
-            const double v = Ud[k] + ((double)ah + (double)al);
-            static_cast<double*>(hout)[idx] = v;
-            if (k == 0) bad |= !(v > 0.0);
-        }
-    }
-    if (bad) {
-        atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
-        atomicOr(&A.item_flags[tile.dom], SHLL_FLAG_NONPOSITIVE);
-    }
-}
-
-// applies the last step's edge corrections to the edge cells (after the final step of a run)
-template <bool KAHAN>
-__global__ void k_fixup2d(Args2 A, int ndom) {
-    const int d = blockIdx.y;
-    if (d >= ndom) return;
-    const Dom2 D = A.doms[d];
-    if (D.steps <= 0) return;
-    const long ncell = (long)D.nx * D.ny;
-    const int buf = (D.par + D.steps) & 1;
-    void* h = buf ? A.hi[1] : A.hi[0];
-    float* l = buf ? A.lo[1] : A.lo[0];
-    Args2 B = A;
-    B.step = D.steps;  // corrections of step D.steps - 1
-    for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c / D.ny), j = (int)(c % D.ny);
-        if (!((i > 0 && i % TI == 0) || (j > 0 && j % TJ == 0))) continue;
-        double corr[4];
-        cell_correction(B, D, i, j, corr);
-        for (int k = 0; k < 4; k++) {
-            const long idx = k * A.plane + D.base + c;
-            if (KAHAN) {
-                float* hh = static_cast<float*>(h);
-                const double v = ((double)hh[idx] + (double)l[idx]) + corr[k];
-                split2(v, hh[idx], l[idx]);
-            } else {
-                static_cast<double*>(h)[idx] += corr[k];
-            }
-        }
+        pho[k * P + cell] = ah;
+        plo[k * P + cell] = al;
     }
 }
 
@@ -415,17 +462,22 @@ __global__ void k_fixup2d(Args2 A, int ndom) {
 struct Mixed2D {
     std::vector<Dom2> doms;
     std::vector<TileD> tiles;
-    std::vector<int> par;
     long plane = 0, nex = 0, ney = 0;
-    void* hi[2] = {nullptr, nullptr};
-    float* lo[2] = {nullptr, nullptr};
+    void* B = nullptr;
+    float* Blo = nullptr;
+    float* C = nullptr;
+    float* Ph[2] = {nullptr, nullptr};
+    float* Pl[2] = {nullptr, nullptr};
     Edge* ex[2] = {nullptr, nullptr};
     Edge* ey[2] = {nullptr, nullptr};
+    Frame2* frames = nullptr;
     Dom2* d_doms = nullptr;
     TileD* d_tiles = nullptr;
+    int fold = 16;
 };
 
 static Mixed2D* get2(MixedState* m) { return static_cast<Mixed2D*>(*mixed_d2_slot(m)); }
+int mixed_fold(MixedState* m);
 
 MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
     int count = 0;
@@ -438,18 +490,20 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
     }
     Mixed2D* d = new Mixed2D();
     *mixed_d2_slot(m) = d;
-    long off = 0, oex = 0, oey = 0;
+    d->fold = std::max(1, mixed_fold(m));
+    long off = 0, oex = 0, oey = 0, otile = 0;
     for (int t = 0; t < count; t++) {
         const shll_params& p = items[t];
         Dom2 D;
         memset(&D, 0, sizeof(D));
-        D.base = off;
+        D.base = (int)off;
         D.nx = p.nx;
         D.ny = p.ny;
         D.tiles_i = (p.nx + TI - 1) / TI;
         D.tiles_j = (p.ny + TJ - 1) / TJ;
-        D.ex_base = oex;
-        D.ey_base = oey;
+        D.tile_base = (int)otile;
+        D.ex_base = (int)oex;
+        D.ey_base = (int)oey;
         D.gamma = p.gamma;
         D.R = p.R;
         D.CV = p.R / (p.gamma - 1.0);
@@ -457,25 +511,37 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
         const double dt = (p.cfl / (p.R + 1)) * dx;
         D.lamx = p.cfl / (p.R + 1);
         D.lamy = dt / dy;
+        D.lxh = (float)D.lamx; D.lxl = (float)(D.lamx - (double)D.lxh);
+        D.lyh = (float)D.lamy; D.lyl = (float)(D.lamy - (double)D.lyh);
         d->doms.push_back(D);
         for (int a = 0; a < D.tiles_i; a++)
             for (int b = 0; b < D.tiles_j; b++) d->tiles.push_back({t, a, b});
         off += (long)p.nx * p.ny;
+        otile += (long)D.tiles_i * D.tiles_j;
         oex += (long)(D.tiles_i - 1) * p.ny;
         oey += (long)(D.tiles_j - 1) * p.nx;
+    }
+    if (4 * off >= (1L << 31) || oex >= (1L << 31) || oey >= (1L << 31)) {
+        snprintf(err, len, "2D mixed: %ld cells exceed the 2^29-cell limit of a batch", off);
+        delete d;
+        *mixed_d2_slot(m) = nullptr;
+        return nullptr;
     }
     d->plane = off;
     d->nex = std::max(oex, 1L);
     d->ney = std::max(oey, 1L);
-    d->par.assign(count, 0);
     const bool kahan = mixed_is_kahan(m);
-    bool ok = true;
+    const size_t nf = (size_t)4 * off;
+    bool ok = cudaMalloc(&d->B, nf * (kahan ? sizeof(float) : sizeof(double))) == cudaSuccess;
+    if (ok && kahan) ok = cudaMalloc(&d->Blo, nf * sizeof(float)) == cudaSuccess;
+    if (ok) ok = cudaMalloc(&d->C, nf * sizeof(float)) == cudaSuccess;
     for (int b = 0; b < 2 && ok; b++) {
-        ok = cudaMalloc(&d->hi[b], (size_t)4 * off * (kahan ? sizeof(float) : sizeof(double))) == cudaSuccess;
-        if (ok && kahan) ok = cudaMalloc(&d->lo[b], (size_t)4 * off * sizeof(float)) == cudaSuccess;
+        ok = cudaMalloc(&d->Ph[b], nf * sizeof(float)) == cudaSuccess;
+        if (ok) ok = cudaMalloc(&d->Pl[b], nf * sizeof(float)) == cudaSuccess;
         if (ok) ok = cudaMalloc(&d->ex[b], sizeof(Edge) * d->nex) == cudaSuccess;
         if (ok) ok = cudaMalloc(&d->ey[b], sizeof(Edge) * d->ney) == cudaSuccess;
     }
+    if (ok) ok = cudaMalloc(&d->frames, sizeof(Frame2) * d->tiles.size()) == cudaSuccess;
     if (ok) ok = cudaMalloc(&d->d_doms, sizeof(Dom2) * count) == cudaSuccess;
     if (ok) ok = cudaMalloc(&d->d_tiles, sizeof(TileD) * d->tiles.size()) == cudaSuccess;
     if (ok) ok = cudaMemcpy(d->d_tiles, d->tiles.data(), sizeof(TileD) * d->tiles.size(), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -490,7 +556,9 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
 void mixed2d_detach(MixedState* m) {
     Mixed2D* d = get2(m);
     if (!d) return;
-    for (int b = 0; b < 2; b++) { cudaFree(d->hi[b]); cudaFree(d->lo[b]); cudaFree(d->ex[b]); cudaFree(d->ey[b]); }
+    cudaFree(d->B); cudaFree(d->Blo); cudaFree(d->C);
+    for (int b = 0; b < 2; b++) { cudaFree(d->Ph[b]); cudaFree(d->Pl[b]); cudaFree(d->ex[b]); cudaFree(d->ey[b]); }
+    cudaFree(d->frames);
     cudaFree(d->d_doms);
     cudaFree(d->d_tiles);
     delete d;
@@ -510,7 +578,6 @@ int mixed2d_load(MixedState* m, int item, const double* prim, char* err, size_t 
         U[2 * n + c] = p0 * p2;
         U[3 * n + c] = p0 * (p3 * D.CV + 0.5 * (p1 * p1 + p2 * p2));
     }
-    d->par[item] = 0;
     cudaStream_t s = mixed_stream(m);
     for (int k = 0; k < 4; k++) {
         const size_t off = (size_t)k * d->plane + D.base;
@@ -521,11 +588,11 @@ int mixed2d_load(MixedState* m, int item, const double* prim, char* err, size_t 
                 h[c] = (float)U[k * n + c];
                 l[c] = (float)(U[k * n + c] - (double)h[c]);
             }
-            e = cudaMemcpyAsync(static_cast<float*>(d->hi[0]) + off, h.data(), n * sizeof(float), cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(d->lo[0] + off, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(static_cast<float*>(d->B) + off, h.data(), n * sizeof(float), cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d->Blo + off, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         } else {
-            e = cudaMemcpyAsync(static_cast<double*>(d->hi[0]) + off, U.data() + k * n, n * sizeof(double),
+            e = cudaMemcpyAsync(static_cast<double*>(d->B) + off, U.data() + k * n, n * sizeof(double),
                                 cudaMemcpyHostToDevice, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         }
@@ -542,7 +609,6 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
     for (int t = 0; t < count; t++) {
         const long s = nsteps >= 0 ? nsteps : shll_steps_for(&items[t]);
         d->doms[t].steps = (int)s;
-        d->doms[t].par = d->par[t];
         maxsteps = std::max(maxsteps, s);
         updates += s * (long)d->doms[t].nx * d->doms[t].ny;
     }
@@ -553,29 +619,44 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
         return SHLL_ERR_CUDA;
     }
     Args2 A;
+    memset(&A, 0, sizeof(A));
     A.doms = d->d_doms;
     A.tiles = d->d_tiles;
-    A.hi[0] = d->hi[0]; A.hi[1] = d->hi[1];
-    A.lo[0] = d->lo[0]; A.lo[1] = d->lo[1];
+    A.frames = d->frames;
+    A.B = d->B; A.Blo = d->Blo; A.C = d->C;
+    A.Ph[0] = d->Ph[0]; A.Ph[1] = d->Ph[1];
+    A.Pl[0] = d->Pl[0]; A.Pl[1] = d->Pl[1];
     A.ex[0] = d->ex[0]; A.ex[1] = d->ex[1];
     A.ey[0] = d->ey[0]; A.ey[1] = d->ey[1];
-    A.plane = d->plane;
+    A.plane = (int)d->plane;
     A.flag = mixed_flag_ptr(m);
     A.item_flags = mixed_item_flags_ptr(m);
     const bool kahan = mixed_is_kahan(m);
     const int ntiles = (int)d->tiles.size();
-    shll_count_launches(maxsteps + 1);
+    long launches = 0;
+    auto fold = [&](int s0, int win) {
+        A.s0 = s0;
+        A.win = win;
+        if (kahan) k_fold2d<true><<<ntiles, NT, 0, s>>>(A);
+        else k_fold2d<false><<<ntiles, NT, 0, s>>>(A);
+        launches++;
+    };
+    fold(0, 0);  // frames and C of the current state
+    int s0 = 0;
     for (long st = 0; st < maxsteps; st++) {
         A.step = (int)st;
+        A.s0 = s0;
         if (kahan) k_step2d<true><<<ntiles, NT, 0, s>>>(A);
         else k_step2d<false><<<ntiles, NT, 0, s>>>(A);
+        launches++;
+        if (st + 1 - s0 == d->fold || st + 1 == maxsteps) {
+            fold(s0, (int)(st + 1 - s0));
+            s0 = (int)(st + 1);
+        }
     }
-    dim3 fg(256, count);
-    if (kahan) k_fixup2d<true><<<fg, 256, 0, s>>>(A, count);
-    else k_fixup2d<false><<<fg, 256, 0, s>>>(A, count);
+    shll_count_launches(launches);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { snprintf(err, len, "2D step launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
-    for (int t = 0; t < count; t++) d->par[t] = (d->par[t] + d->doms[t].steps) & 1;
     mixed_add_updates(m, updates);
     return SHLL_OK;
 }
@@ -584,19 +665,18 @@ int mixed2d_item_conserved(MixedState* m, int item, double* planes, char* err, s
     Mixed2D* d = get2(m);
     const Dom2& D = d->doms[item];
     const size_t n = (size_t)D.nx * D.ny;
-    const int b = d->par[item];
     cudaStream_t s = mixed_stream(m);
     for (int k = 0; k < 4; k++) {
         const size_t off = (size_t)k * d->plane + D.base;
         cudaError_t e;
         if (mixed_is_kahan(m)) {
             std::vector<float> h(n), l(n);
-            e = cudaMemcpyAsync(h.data(), static_cast<float*>(d->hi[b]) + off, n * sizeof(float), cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(l.data(), d->lo[b] + off, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+            e = cudaMemcpyAsync(h.data(), static_cast<float*>(d->B) + off, n * sizeof(float), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(l.data(), d->Blo + off, n * sizeof(float), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
             for (size_t c = 0; c < n; c++) planes[k * n + c] = (double)h[c] + (double)l[c];
         } else {
-            e = cudaMemcpyAsync(planes + k * n, static_cast<double*>(d->hi[b]) + off, n * sizeof(double),
+            e = cudaMemcpyAsync(planes + k * n, static_cast<double*>(d->B) + off, n * sizeof(double),
                                 cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         }
@@ -609,13 +689,12 @@ int mixed2d_totals(MixedState* m, int item, double* out, char* err, size_t len) 
     Mixed2D* d = get2(m);
     const Dom2& D = d->doms[item];
     const long n = (long)D.nx * D.ny;
-    const int b = d->par[item];
     cudaStream_t s = mixed_stream(m);
     for (int k = 0; k < 4; k++) {
         const size_t off = (size_t)k * d->plane + D.base;
         cudaError_t e = mixed_is_kahan(m)
-            ? device_pair_sums(static_cast<float*>(d->hi[b]) + off, d->lo[b] + off, 1, n, &out[k], s)
-            : device_plane_sums(static_cast<double*>(d->hi[b]) + off, 64, 1, n, &out[k], s);
+            ? device_pair_sums(static_cast<float*>(d->B) + off, d->Blo + off, 1, n, &out[k], s)
+            : device_plane_sums(static_cast<double*>(d->B) + off, 64, 1, n, &out[k], s);
         if (e != cudaSuccess) { snprintf(err, len, "2D totals failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     }
     return SHLL_OK;
