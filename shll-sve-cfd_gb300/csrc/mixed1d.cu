@@ -39,8 +39,7 @@
 namespace {
 
 constexpr int MW = 512;       // window capacity (cells) of one CTA
-constexpr int MC = 1;         // cells per thread
-constexpr int MT = MW / MC;   // threads per CTA
+constexpr int MT = MW / 2;    // threads per CTA: two adjacent cells per thread (FP32x2 lanes)
 
 struct TubeP {
     long base;        // offset of cell 0 in the planes
@@ -48,7 +47,9 @@ struct TubeP {
     int steps;        // steps of the current run
     int par;          // buffer holding the tube's state at the start of the run
     double gamma, R, CV, lam;
+    double RoCV;      // R / CV: P = (R/CV) (E - m u / 2)
     float alpha;
+    float gRf, Rf, cvinvf;  // gamma R, R, 1/CV in FP32
     int lam_pow2;     // lam is a power of two: lam*Delta is exact in FP32
 };
 
@@ -67,27 +68,51 @@ struct Frame1 {
     float Uh[3], Ul[3];  // anchor as an FP32 pair
 };
 
-__device__ void make_frame(Frame1& f, const double U[3], const TubeP& tp) {
-    double rho = U[0], m = U[1], E = U[2];
-    double u = m / rho, e = E / rho;
-    double T = (e - 0.5 * u * u) / tp.CV;
-    double a = sqrt(tp.gamma * tp.R * T);
-    double M = u / a, P = rho * tp.R * T;
-    double Z1 = 0.5 * (M + 1.0), Z2 = 0.5 * a * (1.0 - M * M), Z3 = 0.5 * (M - 1.0);
-    double F[3] = {m, m * u + P, u * (E + P)};
+// Frame of an anchor state.  FP64 only where the frame's values enter the state directly: the
+// anchor flux F (boundary-flux sums, walls) and, for first-order wall chunks, the wall split
+// fluxes fpS1/fmS1.  1/rho and 1/a come from FP32 seeds refined by Newton steps in FP64
+// (r <- r (2 - rho r) doubles the correct bits: 2^-22 -> 2^-44 -> 2^-88).  The FP32
+// coefficients only multiply deviations, so FP32 accuracy suffices for them.  Run by one thread:
+// every FP64 operation costs a full warp slot of the narrow FP64 pipe, so their number is kept
+// small (about 15, plus 15 for wall chunks of first order).
+__device__ void make_frame(Frame1& f, const double U[3], const TubeP& tp, bool wall_fluxes) {
+    const double rho = U[0], m = U[1], E = U[2];
+    double r = f2d_bits(fast_rcp(d2f_bits(rho)));
+    r = fma(r, fma(-rho, r, 1.0), r);
+    r = fma(r, fma(-rho, r, 1.0), r);
+    const double u0 = m * r;
+    const double u = fma(r, fma(-rho, u0, m), u0);
+    const double P = tp.RoCV * fma(-0.5 * m, u, E);
+    const double F[3] = {m, fma(m, u, P), u * (E + P)};
     for (int k = 0; k < 3; k++) {
         f.U[k] = U[k];
         f.F[k] = F[k];
-        f.c.F[k] = (float)F[k];
-        f.c.Uf[k] = (float)U[k];
-        f.Uh[k] = (float)U[k];
-        f.Ul[k] = (float)(U[k] - (double)f.Uh[k]);
+        f.c.F[k] = d2f_bits(F[k]);
+        d2ff_bits(U[k], f.Uh[k], f.Ul[k]);
+        f.c.Uf[k] = f.Uh[k];
     }
-    f.fpS1 = F[1] * Z1 + m * Z2;
-    f.fmS1 = -F[1] * Z3 - m * Z2;
-    f.c.rho = (float)rho; f.c.u = (float)u; f.c.v = 0.f; f.c.e = (float)e; f.c.T = (float)T; f.c.a = (float)a;
-    f.c.M = (float)M; f.c.P = (float)P; f.c.Z1 = (float)Z1; f.c.Z2 = (float)Z2;
-    f.c.gR = (float)(tp.gamma * tp.R); f.c.R = (float)tp.R; f.c.cvinv = (float)(1.0 / tp.CV);
+    const float rf = d2f_bits(r), uf = d2f_bits(u), Pf = d2f_bits(P);
+    const float Tf = __fmul_rn(__fmul_rn(Pf, rf), fast_rcp(tp.Rf));
+    const float a2 = __fmul_rn(tp.gRf, Tf);
+    const float ainv = rsqrtf(a2);
+    const float af = __fmul_rn(a2, ainv);
+    const float Mf = __fmul_rn(uf, ainv);
+    f.c.rho = d2f_bits(rho); f.c.u = uf; f.c.v = 0.f; f.c.e = __fmul_rn(f.c.Uf[2], rf); f.c.T = Tf;
+    f.c.a = af; f.c.M = Mf; f.c.P = Pf; f.c.Z1 = __fmul_rn(0.5f, __fadd_rn(Mf, 1.0f));
+    f.c.Z2 = __fmul_rn(__fmul_rn(0.5f, af), __fmaf_rn(-Mf, Mf, 1.0f));
+    f.c.gR = tp.gRf; f.c.R = tp.Rf; f.c.cvinv = tp.cvinvf;
+    f.fpS1 = f.fmS1 = 0.0;
+    if (wall_fluxes) {  // a^2 = gamma P / rho; y = 1/a by Newton steps y <- y (3/2 - a^2 y^2 / 2)
+        const double A2 = tp.gamma * P * r;
+        double y = f2d_bits(rsqrtf(d2f_bits(A2)));
+        const double h = 0.5 * A2;
+        y = y * fma(-h * y, y, 1.5);
+        y = y * fma(-h * y, y, 1.5);
+        const double a = A2 * y, M = u * y;
+        const double Z1 = fma(0.5, M, 0.5), Z3 = Z1 - 1.0, Z2 = 0.5 * a * fma(-M, M, 1.0);
+        f.fpS1 = fma(F[1], Z1, m * Z2);
+        f.fmS1 = -fma(F[1], Z3, m * Z2);
+    }
 }
 
 // reads the stored state of tube cell i as FP64 (F64 planes, or an FP32 pair)
@@ -123,18 +148,28 @@ __device__ __forceinline__ double boundary_correction(const BSum* bs, int left, 
 
 struct Smem1 {
     Frame1 fr;
-    alignas(16) float sfp[3][MW];
-    alignas(16) float sfm[3][MW];
-    float sTh[3][MT], sTl[3][MT];       // lam*Delta of each thread's last interface (FP32 pair)
+    alignas(16) float sfp[2][3][MW];    // split-flux deviations, double-buffered by step parity
+    alignas(16) float sfm[2][3][MW];
     float wall[2][3][2];                // constant wall terms (order 1) for cell 0 / n-1
     double corr[2][3];                  // boundary corrections of cells a and b (previous sweep)
 };
 
+// lane q of a float2
+__device__ __forceinline__ float lane(float2 v, int q) { return q ? v.y : v.x; }
+__device__ __forceinline__ void set_lane(float2& v, int q, float x) { if (q) v.y = x; else v.x = x; }
+
+// One sweep of one chunk.  Thread t holds window cells w0 = 2t and w0 + 1 as the two lanes of
+// FP32x2 registers.  Per step: split-flux deviations of both cells (packed) -> shared memory
+// (buffer of the step's parity) -> one barrier -> the thread evaluates the three interfaces
+// w0-1/2, w0+1/2, w0+3/2 that its cells need (the outer two are also evaluated, bit for bit
+// identically, by the neighbouring threads) -> TwoSum accumulation of lam*(F_in - F_out).
+// The double buffer makes the second barrier of a store/load/store pattern unnecessary: a
+// thread can only overwrite a buffer after every thread has passed the barrier that follows
+// the last reads of it.
 template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
 __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp, Smem1& S) {
     constexpr int R_ = ORDER;  // stencil reach per step
     Frame1& fr = S.fr;
-    auto& sfp = S.sfp; auto& sfm = S.sfm; auto& sTh = S.sTh; auto& sTl = S.sTl; auto& wall = S.wall;
 
     const int tid = threadIdx.x;
     const int n = tp.n;
@@ -156,6 +191,30 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         if (tid == 0) atomicOr(A.flag, SHLL_FLAG_BADARG);
         return;
     }
+    // the window's stored values, loaded first so that their latency overlaps the frame setup
+    const int w0 = 2 * tid;
+    double uin[2][3];           // FP64 state
+    float uh[2][3], ul[2][3];   // FP32 value + compensation (KAHAN)
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            uin[q][k] = 0.0; uh[q][k] = 0.f; ul[q][k] = 0.f;
+            const int w = w0 + q;
+            if (w < L) {
+                const long idx = k * P + base + ws + w;
+                if (KAHAN) { uh[q][k] = static_cast<const float*>(hin)[idx]; ul[q][k] = lin[idx]; }
+                else uin[q][k] = static_cast<const double*>(hin)[idx];
+            }
+        }
+    double Uanc[3];
+    float Uanc_h[3], Uanc_l[3];
+    if (tid == 0)
+        for (int k = 0; k < 3; k++) {
+            const long idx = k * P + base + ch.anc;
+            if (KAHAN) { Uanc_h[k] = static_cast<const float*>(hin)[idx]; Uanc_l[k] = lin[idx]; }
+            else Uanc[k] = static_cast<const double*>(hin)[idx];
+        }
     // corrections of the previous sweep for cell a (from the left neighbour) and cell b (the right
     // neighbour's first cell, which lies in this window's halo)
     if (tid < 6) {
@@ -171,12 +230,15 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     __syncthreads();
     if (tid == 0) {
         double U[3];
+        const bool corrected = ch.anc == ch.a || ch.anc == ch.b;
         for (int k = 0; k < 3; k++) {
-            U[k] = load_state<KAHAN>(hin, lin, k * P + base + ch.anc);
+            U[k] = KAHAN ? f2d_bits(Uanc_h[k]) + f2d_bits(Uanc_l[k]) : Uanc[k];
             if (ch.anc == ch.a) U[k] += S.corr[0][k];
             if (ch.anc == ch.b) U[k] += S.corr[1][k];
         }
-        make_frame(fr, U, tp);
+        make_frame(fr, U, tp, ORDER == 1 && (ch.idL < 0 || ch.idR < 0));
+        if (KAHAN && !corrected)  // the stored pair itself, so that the anchor cell's deviation is exactly 0
+            for (int k = 0; k < 3; k++) { fr.Uh[k] = Uanc_h[k]; fr.Ul[k] = Uanc_l[k]; }
     }
     __syncthreads();
     if (tid < 6 && ORDER == 1) {
@@ -186,145 +248,148 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         const int bnd = tid / 3, k = tid % 3;
         double w = bnd == 0 ? (k == 1 ? lam * (2.0 * fr.fmS1 - fr.F[1]) : -lam * fr.F[k])
                             : (k == 1 ? lam * (fr.F[1] - 2.0 * fr.fpS1) : lam * fr.F[k]);
-        split2(w, wall[bnd][k][0], wall[bnd][k][1]);
+        d2ff_bits(w, S.wall[bnd][k][0], S.wall[bnd][k][1]);
     }
 
-    // ---- load the window as deviations from the frame ----
-    const int w0 = tid * MC;
-    float dh[MC][3], dl[MC][3];
+    // ---- the window as deviations from the frame ----
+    float2 dh[3], dl[3];
 #pragma unroll
-    for (int q = 0; q < MC; q++) {
+    for (int q = 0; q < 2; q++) {
         const int w = w0 + q;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            dh[q][k] = 0.f; dl[q][k] = 0.f;
+            float h = 0.f, l = 0.f;
             if (w < L) {
-                const long idx = k * P + base + ws + w;
                 const bool corrected = w == pa || w == pb;  // cells owed a boundary correction
                 if (KAHAN) {
-                    const float h = static_cast<const float*>(hin)[idx], l = lin[idx];
+                    const float vh = uh[q][k], vl = ul[q][k];
                     if (corrected) {
-                        const double d = ((double)h - fr.U[k]) + (double)l + S.corr[w == pa ? 0 : 1][k];
-                        split2(d, dh[q][k], dl[q][k]);
+                        const double d = ((f2d_bits(vh) - fr.U[k]) + f2d_bits(vl)) + S.corr[w == pa ? 0 : 1][k];
+                        d2ff_bits(d, h, l);
                     } else {
-                        ff_sub(h, l, fr.Uh[k], fr.Ul[k], dh[q][k], dl[q][k]);
+                        ff_sub(vh, vl, fr.Uh[k], fr.Ul[k], h, l);
                     }
                 } else {
-                    double d = static_cast<const double*>(hin)[idx] - fr.U[k];
+                    double d = uin[q][k] - fr.U[k];
                     if (corrected) d += S.corr[w == pa ? 0 : 1][k];
-                    split2(d, dh[q][k], dl[q][k]);
+                    d2ff_bits(d, h, l);
                 }
             }
+            set_lane(dh[k], q, h);
+            set_lane(dl[k], q, l);
         }
     }
+    const Coef2 c2 = coef2(fr.c);
+    const float2 lamh2 = f2(lamh), laml2 = f2(laml);
     // flux sums at the chunk's two boundary interfaces (kept by the threads that apply them)
     float bh[2][3] = {{0, 0, 0}, {0, 0, 0}}, bl[2][3] = {{0, 0, 0}, {0, 0, 0}};
     const bool hasL = ch.idL >= 0, hasR = ch.idR >= 0;
-    // loop-invariant roles of this thread's cells
-    bool in_ok[MC], out_ok[MC], sp0[MC], sm0[MC], special[MC];
+    // loop-invariant roles of this thread's cells (i = tube cell of window cell w)
+    auto edge = [&](int w) { const int i = ws + w; return i == 0 || i == n - 1; };
+    // half-slope factors: 0.5, or 0 on edge cells (the reference's zero slopes there)
+    const float2 hp = make_float2(edge(w0) ? 0.f : 0.5f, edge(w0 + 1) ? 0.f : 0.5f);
+    const float2 nhm = neg2(hp);
+    const float hpl = edge(w0 - 1) ? 0.f : 0.5f;    // cell w0 - 1 (sp only)
+    const float nhmr = edge(w0 + 2) ? -0.f : -0.5f; // cell w0 + 2 (sm only)
+    // interface masks: a cell's left / right interface is applied unless it is a wall (the wall
+    // term replaces it) or lies outside the window
+    auto in_ok = [&](int w) { const int i = ws + w; return i > 0 && w > 0 && w < L; };
+    auto out_ok = [&](int w) { const int i = ws + w; return i < n - 1 && w < L - 1; };
+    const float2 inm = make_float2(in_ok(w0) ? 1.f : 0.f, in_ok(w0 + 1) ? 1.f : 0.f);
+    const float2 outm = make_float2(out_ok(w0) ? 1.f : 0.f, out_ok(w0 + 1) ? 1.f : 0.f);
+    bool special[2];
 #pragma unroll
-    for (int q = 0; q < MC; q++) {
+    for (int q = 0; q < 2; q++) {
         const int w = w0 + q, i = ws + w;
-        in_ok[q] = i > 0 && w > 0 && w < L;
-        out_ok[q] = i < n - 1 && w < L - 1;
-        sp0[q] = i == 0 || i == n - 1;          // dfp of cell i is zero (edge cell)
-        sm0[q] = i + 1 == n - 1;                // dfm of cell i+1 is zero
         special[q] = w < L && (i == 0 || i == n - 1 || (w == pa && hasL) || (w == pb - 1 && hasR));
     }
+    const bool any_special = special[0] || special[1];
+    const int jl = max(w0 - 2, 0), jr = min(w0 + 2, MW - 2);  // neighbour pairs (clamped)
 
     for (int s = 0; s < steps; s++) {
-        // ---- A: split-flux deviations ----
-        float fp[MC][3], fm[MC][3];
+        const int b = s & 1;
+        // ---- split-flux deviations of both cells ----
+        float2 fp[3], fm[3];
+        {
+            float2 d[3];
 #pragma unroll
-        for (int q = 0; q < MC; q++) {
-            float d[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) d[k] = __fadd_rn(dh[q][k], dl[q][k]);
-            dflux1(fr.c, d, fp[q], fm[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < MC; q++)
-#pragma unroll
-            for (int k = 0; k < 3; k++) { sfp[k][w0 + q] = fp[q][k]; sfm[k][w0 + q] = fm[q][k]; }
-        __syncthreads();
-        // ---- B: interface terms lam*Delta_{j+1/2}, j = w0..w0+MC-1 ----
-        float th[MC][3], tl[MC][3];
-        float pl[3], pr[2][3], mr[2][3];
-        {   // neighbours' values (clamped at the window ends, whose cells are in the halo)
-            const int cl = max(w0 - 1, 0), cr0 = min(w0 + MC, MW - 1), cr1 = min(w0 + MC + 1, MW - 1);
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                if (ORDER == 2) { pl[k] = sfp[k][cl]; pr[0][k] = sfp[k][cr0]; mr[1][k] = sfm[k][cr1]; }
-                mr[0][k] = sfm[k][cr0];
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < MC; q++) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                float Dl;
-                const float p1 = fp[q][k];
-                const float m2 = q + 1 < MC ? fm[q + 1][k] : mr[0][k];
-                if (ORDER == 1) {
-                    Dl = __fadd_rn(p1, m2);
-                } else {
-                    const float p0 = q > 0 ? fp[q - 1][k] : pl[k];
-                    const float p2 = q + 1 < MC ? fp[q + 1][k] : pr[0][k];
-                    const float m1 = fm[q][k];
-                    const float m3 = q + 2 < MC ? fm[q + 2][k] : mr[q + 2 - MC][k];
-                    const float sp = sp0[q] ? 0.f : slope_f<LIM>(p0, p1, p2, tp.alpha);
-                    const float sm = sm0[q] ? 0.f : slope_f<LIM>(m1, m2, m3, tp.alpha);
-                    Dl = __fadd_rn(__fadd_rn(__fadd_rn(p1, __fmul_rn(0.5f, sp)), m2), -__fmul_rn(0.5f, sm));
-                }
-                th[q][k] = __fmul_rn(lamh, Dl);
-                tl[q][k] = LAM_POW2 ? 0.f : __fadd_rn(__fmaf_rn(lamh, Dl, -th[q][k]), __fmul_rn(laml, Dl));
-            }
+            for (int k = 0; k < 3; k++) d[k] = add2(dh[k], dl[k]);
+            dflux1x2(c2, d, fp, fm);
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            sTh[k][tid] = th[MC - 1][k];
-            if (!LAM_POW2) sTl[k][tid] = tl[MC - 1][k];
+            *reinterpret_cast<float2*>(&S.sfp[b][k][w0]) = fp[k];
+            *reinterpret_cast<float2*>(&S.sfm[b][k][w0]) = fm[k];
         }
         __syncthreads();
-        // ---- C: accumulate lam*(F_{i-1/2} - F_{i+1/2}) per cell ----
-        const int tl_ = max(tid - 1, 0);
+        // ---- interfaces w0-1/2 (IN.x), w0+1/2 (IN.y = OUT.x), w0+3/2 (OUT.y) ----
 #pragma unroll
-        for (int q = 0; q < MC; q++) {
+        for (int k = 0; k < 3; k++) {
+            const float2 pL = *reinterpret_cast<const float2*>(&S.sfp[b][k][jl]);  // fp_{w0-2}, fp_{w0-1}
+            const float2 mR = *reinterpret_cast<const float2*>(&S.sfm[b][k][jr]);  // fm_{w0+2}, fm_{w0+3}
+            float2 IN, OUT;
+            if (ORDER == 1) {
+                IN = add2(make_float2(pL.y, fp[k].x), fm[k]);
+                OUT = add2(fp[k], make_float2(fm[k].y, mR.x));
+            } else {
+                const float2 pR = *reinterpret_cast<const float2*>(&S.sfp[b][k][jr]);  // fp_{w0+2}
+                const float2 mL = *reinterpret_cast<const float2*>(&S.sfm[b][k][jl]);  // fm_{w0-1}
+                // differences f_j - f_{j-1}
+                const float2 dpo = sub2(fp[k], make_float2(pL.y, fp[k].x));     // j = w0, w0+1
+                const float2 dpr = sub2(make_float2(fp[k].y, pR.x), fp[k]);     // j = w0+1, w0+2
+                const float dpl = __fadd_rn(pL.y, -pL.x);                        // j = w0-1
+                const float2 dmo = sub2(fm[k], make_float2(mL.y, fm[k].x));
+                const float2 dmr = sub2(make_float2(fm[k].y, mR.x), fm[k]);
+                const float dmrr = __fadd_rn(mR.y, -mR.x);                       // j = w0+3
+                // reconstructed left states L_j = fp_j + sp_j/2 and right states R_j = fm_j - sm_j/2
+                const float2 Lo = fma2(hp, slope2<LIM>(dpo, dpr, tp.alpha), fp[k]);           // j = w0, w0+1
+                const float Ll = __fmaf_rn(hpl, slope_s<LIM>(dpl, dpo.x, tp.alpha), pL.y);      // j = w0-1
+                const float2 Ro = fma2(nhm, slope2<LIM>(dmo, dmr, tp.alpha), fm[k]);          // j = w0, w0+1
+                const float Rr = __fmaf_rn(nhmr, slope_s<LIM>(dmr.y, dmrr, tp.alpha), mR.x);    // j = w0+2
+                IN = add2(make_float2(Ll, Lo.x), Ro);
+                OUT = add2(Lo, make_float2(Ro.y, Rr));
+            }
+            float2 ih = mul2(lamh2, IN), oh = mul2(lamh2, OUT);
+            float2 il = f2(0.f), ol = f2(0.f);
+            if (!LAM_POW2) {
+                il = add2(fma2(lamh2, IN, neg2(ih)), mul2(laml2, IN));
+                ol = add2(fma2(lamh2, OUT, neg2(oh)), mul2(laml2, OUT));
+            }
+            ih = mul2(ih, inm); oh = mul2(oh, outm);
+            two_sum_acc2(dh[k], dl[k], ih);
+            two_sum_acc2(dh[k], dl[k], neg2(oh));
+            if (!LAM_POW2) {
+                il = mul2(il, inm); ol = mul2(ol, outm);
+                dl[k] = add2(dl[k], sub2(il, ol));
+            }
+            if (any_special) {
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                float ih = q > 0 ? th[q - 1][k] : sTh[k][tl_];
-                float il = LAM_POW2 ? 0.f : (q > 0 ? tl[q - 1][k] : sTl[k][tl_]);
-                ih = in_ok[q] ? ih : 0.f;
-                il = in_ok[q] ? il : 0.f;
-                const float oh = out_ok[q] ? th[q][k] : 0.f;
-                const float ol = out_ok[q] ? tl[q][k] : 0.f;
-                two_sum_acc(dh[q][k], dl[q][k], ih);
-                two_sum_acc(dh[q][k], dl[q][k], -oh);
-                if (!LAM_POW2) dl[q][k] = __fadd_rn(dl[q][k], __fadd_rn(il, -ol));
-                if (special[q]) {
+                for (int q = 0; q < 2; q++) {
+                    if (!special[q]) continue;
                     const int w = w0 + q, i = ws + w;
-                    float& h = dh[q][k];
-                    float& l = dl[q][k];
-                    if (w == pa && hasL) { two_sum_acc(bh[0][k], bl[0][k], ih); bl[0][k] = __fadd_rn(bl[0][k], il); }
-                    if (w == pb - 1 && hasR) { two_sum_acc(bh[1][k], bl[1][k], oh); bl[1][k] = __fadd_rn(bl[1][k], ol); }
+                    float h = lane(dh[k], q), l = lane(dl[k], q);
+                    if (w == pa && hasL) { two_sum_acc(bh[0][k], bl[0][k], lane(ih, q)); bl[0][k] = __fadd_rn(bl[0][k], lane(il, q)); }
+                    if (w == pb - 1 && hasR) { two_sum_acc(bh[1][k], bl[1][k], lane(oh, q)); bl[1][k] = __fadd_rn(bl[1][k], lane(ol, q)); }
                     if (i == 0 || i == n - 1) {
                         if (ORDER == 1) {
                             const int bnd = i == 0 ? 0 : 1;
-                            two_sum_acc(h, l, wall[bnd][k][0]); l = __fadd_rn(l, wall[bnd][k][1]);
+                            two_sum_acc(h, l, S.wall[bnd][k][0]); l = __fadd_rn(l, S.wall[bnd][k][1]);
                             if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
-                                const float v = i == 0 ? __fmul_rn(2.f, fm[q][1]) : -__fmul_rn(2.f, fp[q][1]);
+                                const float v = i == 0 ? __fmul_rn(2.f, lane(fm[1], q)) : -__fmul_rn(2.f, lane(fp[1], q));
                                 const float vh = __fmul_rn(lamh, v);
                                 const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
                                 two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                             }
                         } else {  // outflow: F_{-1/2} = Fref + dfp_0 + dfm_0 (and likewise at n-1)
-                            float v = __fadd_rn(fp[q][k], fm[q][k]);
+                            float v = __fadd_rn(lane(fp[k], q), lane(fm[k], q));
                             if (i == n - 1) v = -v;
                             const float vh = __fmul_rn(lamh, v);
                             const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
                             two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                         }
                     }
+                    set_lane(dh[k], q, h);
+                    set_lane(dl[k], q, l);
                 }
             }
         }
@@ -332,12 +397,12 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     // ---- boundary flux sums of this sweep (full flux: steps * lam * Fref + sum lam*Delta) ----
     BSum* bout = ((A.sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
 #pragma unroll
-    for (int q = 0; q < MC; q++) {
+    for (int q = 0; q < 2; q++) {
         const int w = w0 + q;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            if (w == pa && hasL) bout->s[0][k] = steps * lam * fr.F[k] + ((double)bh[0][k] + (double)bl[0][k]);
-            if (w == pb - 1 && hasR) bout->s[1][k] = steps * lam * fr.F[k] + ((double)bh[1][k] + (double)bl[1][k]);
+            if (w == pa && hasL) bout->s[0][k] = steps * lam * fr.F[k] + (f2d_bits(bh[0][k]) + f2d_bits(bl[0][k]));
+            if (w == pb - 1 && hasR) bout->s[1][k] = steps * lam * fr.F[k] + (f2d_bits(bh[1][k]) + f2d_bits(bl[1][k]));
         }
     }
 
@@ -346,28 +411,27 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     void* hout = outb ? A.hi[1] : A.hi[0];
     float* lout = outb ? A.lo[1] : A.lo[0];
 #pragma unroll
-    for (int q = 0; q < MC; q++) {
+    for (int q = 0; q < 2; q++) {
         const int w = w0 + q;
         if (w < pa || w >= pb) continue;
-        double uu[3];
+        float uf[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const long idx = k * P + base + ws + w;
+            const float h = lane(dh[k], q), l = lane(dl[k], q);
             if (KAHAN) {
                 float oh, ol;
-                ff_add(fr.Uh[k], fr.Ul[k], dh[q][k], dl[q][k], oh, ol);
+                ff_add(fr.Uh[k], fr.Ul[k], h, l, oh, ol);
                 static_cast<float*>(hout)[idx] = oh;
                 lout[idx] = ol;
-                uu[k] = (double)oh;
+                uf[k] = oh;
             } else {
-                const double v = fr.U[k] + ((double)dh[q][k] + (double)dl[q][k]);
-                static_cast<double*>(hout)[idx] = v;
-                uu[k] = v;
+                static_cast<double*>(hout)[idx] = fr.U[k] + (f2d_bits(h) + f2d_bits(l));
+                uf[k] = __fadd_rn(fr.Uh[k], h);  // FP32 estimate, for the positivity check only
             }
         }
-        const float r = (float)uu[0], m = (float)uu[1], E = (float)uu[2];
-        const float eint = __fadd_rn(E, -__fmul_rn(0.5f, __fdividef(__fmul_rn(m, m), r)));
-        bad |= !(r > 0.f) || !(eint > 0.f);
+        const float eint = __fadd_rn(uf[2], -__fmul_rn(0.5f, __fdividef(__fmul_rn(uf[1], uf[1]), uf[0])));
+        bad |= !(uf[0] > 0.f) || !(eint > 0.f);
     }
     if (bad) {
         atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
@@ -526,6 +590,30 @@ static void item_consts(const shll_params& p, double* CV, double* lam, double* l
     *lamy = dt / dy;
 }
 
+// device descriptor of one tube (cells from `base` in the planes)
+static TubeP tube_params(const shll_params& p, long base) {
+    TubeP tp;
+    memset(&tp, 0, sizeof(tp));
+    tp.base = base;
+    tp.n = p.nx;
+    tp.order = p.order;
+    tp.limiter = p.limiter;
+    tp.gamma = p.gamma;
+    tp.R = p.R;
+    double lamy;
+    item_consts(p, &tp.CV, &tp.lam, &lamy);
+    tp.RoCV = tp.R / tp.CV;
+    tp.gRf = (float)(tp.gamma * tp.R);
+    tp.Rf = (float)tp.R;
+    tp.cvinvf = (float)(1.0 / tp.CV);
+    tp.alpha = (float)p.mc_alpha;
+    int ex;
+    tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
+    tp.steps = 0;
+    tp.par = 0;
+    return tp;
+}
+
 MixedState* mixed2d_attach(MixedState* m, char* err, size_t len);  // mixed2d.cu
 void mixed2d_detach(MixedState* m);
 int mixed2d_load(MixedState* m, int item, const double* prim, char* err, size_t len);
@@ -572,24 +660,7 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
     long off = 0;
     for (int t = 0; t < count; t++) {
         const shll_params& p = items[t];
-        TubeP tp;
-        memset(&tp, 0, sizeof(tp));
-        tp.base = off;
-        tp.n = p.nx;
-        tp.order = p.order;
-        tp.limiter = p.limiter;
-        tp.gamma = p.gamma;
-        tp.R = p.R;
-        double lamy;
-        item_consts(p, &tp.CV, &tp.lam, &lamy);
-        tp.alpha = (float)p.mc_alpha;
-        {
-            int ex;
-            tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
-        }
-        tp.steps = 0;
-        tp.par = 0;
-        m->tubes.push_back(tp);
+        m->tubes.push_back(tube_params(p, off));
         off += p.nx;
     }
     m->plane = off;
@@ -971,21 +1042,7 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     // descriptors of the tube, built on the stack
     const int fold = p->fold_steps > 0 ? p->fold_steps : 16;
     const int B = std::min(fold, MW / 16);
-    TubeP tp;
-    memset(&tp, 0, sizeof(tp));
-    tp.base = 0;
-    tp.n = p->nx;
-    tp.order = p->order;
-    tp.limiter = p->limiter;
-    tp.gamma = p->gamma;
-    tp.R = p->R;
-    double lamy;
-    item_consts(*p, &tp.CV, &tp.lam, &lamy);
-    tp.alpha = (float)p->mc_alpha;
-    {
-        int ex;
-        tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
-    }
+    TubeP tp = tube_params(*p, 0);
     tp.steps = (int)nsteps;
     tp.par = 0;
     Chunk chunks[kStaticMaxChunks];

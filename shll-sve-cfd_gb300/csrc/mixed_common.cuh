@@ -100,3 +100,149 @@ __device__ __forceinline__ void dflux1(const AnchorCoef& c, const float d[3], fl
         dfm[k] = -__fadd_rn(a3, a2);
     }
 }
+
+// ---- packed FP32x2: two cells per thread, one f32x2 instruction per operation --------------
+// (__fadd2_rn / __fmul2_rn / __ffma2_rn: the sm_100-family packed FP32 instructions, each lane
+// rounded to nearest exactly like the scalar operation, so a packed lane and a scalar evaluation
+// of the same formula give identical bits)
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(fast_rcp(a.x), fast_rcp(a.y)); }
+__device__ __forceinline__ float2 rsqrt2(float2 a) { return make_float2(rsqrtf(a.x), rsqrtf(a.y)); }
+
+// h + l += v per lane (TwoSum)
+__device__ __forceinline__ void two_sum_acc2(float2& h, float2& l, float2 v) {
+    const float2 s = add2(h, v);
+    const float2 bp = sub2(s, h);
+    const float2 e = add2(sub2(h, sub2(s, bp)), sub2(v, bp));
+    h = s;
+    l = add2(l, e);
+}
+
+// minmod(a, b) = max(min(a,b),0) + min(max(a,b),0): the smaller magnitude when a and b have
+// the same sign, else 0 (one of the two terms is always 0, so the sum is exact); symmetric in
+// a and b, so every thread that evaluates the same slope gets the same bits
+__device__ __forceinline__ float minmod_s(float a, float b) {
+    return __fadd_rn(fmaxf(fminf(a, b), 0.f), fminf(fmaxf(a, b), 0.f));
+}
+__device__ __forceinline__ float2 minmod2(float2 a, float2 b) {
+    return add2(make_float2(fmaxf(fminf(a.x, b.x), 0.f), fmaxf(fminf(a.y, b.y), 0.f)),
+                make_float2(fminf(fmaxf(a.x, b.x), 0.f), fminf(fmaxf(a.y, b.y), 0.f)));
+}
+// limited slope from the backward and forward differences a = f_j - f_{j-1}, b = f_{j+1} - f_j:
+// minmod (LIM = 0) or the MC limiter minmod((a+b)/2, alpha minmod(a,b)) (LIM = 1,
+// base-omp/2nd_order_base_shll.c:316-325)
+template <int LIM>
+__device__ __forceinline__ float slope_s(float a, float b, float alpha) {
+    if (LIM == 1) return minmod_s(__fmul_rn(0.5f, __fadd_rn(a, b)), __fmul_rn(alpha, minmod_s(a, b)));
+    return minmod_s(a, b);
+}
+template <int LIM>
+__device__ __forceinline__ float2 slope2(float2 a, float2 b, float alpha) {
+    if (LIM == 1) return minmod2(mul2(f2(0.5f), add2(a, b)), mul2(f2(alpha), minmod2(a, b)));
+    return minmod2(a, b);
+}
+
+// anchor coefficients of a 1D frame, each duplicated into both lanes (negated where the
+// formulas subtract them)
+struct Coef2 {
+    float2 rho, u, nu, ne, T, a, M, nM, Z1, Z2, P, gR, R, cvinv;
+    float2 F[3], Uf[3];
+};
+__device__ __forceinline__ Coef2 coef2(const AnchorCoef& c) {
+    Coef2 k;
+    k.rho = f2(c.rho); k.u = f2(c.u); k.nu = f2(-c.u); k.ne = f2(-c.e); k.T = f2(c.T); k.a = f2(c.a);
+    k.M = f2(c.M); k.nM = f2(-c.M); k.Z1 = f2(c.Z1); k.Z2 = f2(c.Z2); k.P = f2(c.P); k.gR = f2(c.gR);
+    k.R = f2(c.R);
+    k.cvinv = f2(c.cvinv);
+    for (int i = 0; i < 3; i++) { k.F[i] = f2(c.F[i]); k.Uf[i] = f2(c.Uf[i]); }
+    return k;
+}
+
+// dflux1 for two cells at once (same formulas, lane by lane)
+__device__ __forceinline__ void dflux1x2(const Coef2& c, const float2 d[3], float2 dfp[3], float2 dfm[3]) {
+    const float2 drho = d[0], dm = d[1], dE = d[2];
+    const float2 rho = add2(c.rho, drho);
+    const float2 r = rcp2(rho);
+    const float2 du = mul2(fma2(c.nu, drho, dm), r);
+    const float2 u = add2(c.u, du);
+    const float2 de = mul2(fma2(c.ne, drho, dE), r);
+    const float2 dT = mul2(fma2(f2(-0.5f), mul2(add2(u, c.u), du), de), c.cvinv);
+    const float2 T = add2(c.T, dT);
+    const float2 gRT = mul2(c.gR, T);
+    const float2 ainv = rsqrt2(gRT);
+    const float2 a = mul2(gRT, ainv);
+    const float2 da = mul2(mul2(c.gR, dT), rcp2(add2(a, c.a)));
+    const float2 dM = mul2(fma2(c.nM, da, du), ainv);
+    const float2 M = add2(c.M, dM);
+    const float2 dZ1 = mul2(f2(0.5f), dM);
+    const float2 Z1 = add2(c.Z1, dZ1);
+    const float2 Z3 = add2(Z1, f2(-1.0f));
+    const float2 omm = fma2(neg2(M), M, f2(1.0f));
+    const float2 dZ2 = mul2(f2(0.5f), fma2(da, omm, neg2(mul2(mul2(c.a, add2(M, c.M)), dM))));
+    const float2 Z2 = add2(c.Z2, dZ2);
+    const float2 dP = mul2(c.R, fma2(drho, T, mul2(c.rho, dT)));
+    const float2 P = add2(c.P, dP);
+    const float2 E = add2(c.Uf[2], dE);
+    float2 dF[3];
+    dF[0] = dm;
+    dF[1] = add2(fma2(dm, u, mul2(c.Uf[1], du)), dP);
+    dF[2] = fma2(du, add2(E, P), mul2(c.u, add2(dE, dP)));
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float2 a1 = fma2(dF[k], Z1, mul2(c.F[k], dZ1));
+        const float2 a2 = fma2(d[k], Z2, mul2(c.Uf[k], dZ2));
+        const float2 a3 = fma2(dF[k], Z3, mul2(c.F[k], dZ1));
+        dfp[k] = add2(a1, a2);
+        dfm[k] = neg2(add2(a3, a2));
+    }
+}
+
+// ---- FP64 <-> FP32 conversions on the integer pipes --------------------------------------
+// GB300 executes FP64 arithmetic and F2F conversions at 2 lanes per clock per SM, so the
+// once-per-sweep conversions are done with bit operations instead (IEEE-754 layouts:
+// float = s | e8 | m23, double = s | e11 | m52; exponent biases 127 and 1023).
+
+// float -> double, exact for normal floats and zero; subnormal floats become signed zero,
+// infinities and NaNs stay non-finite
+__device__ __forceinline__ double f2d_bits(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    unsigned hi = (b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + ((1023u - 127u) << 20));
+    unsigned lo = b << 29;
+    if (e == 0u) { hi = b & 0x80000000u; lo = 0u; }
+    if (e == 0xffu) hi |= 0x7ff00000u;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> FP32 pair (h, l): h = x truncated to 24 significant bits, l = x - h (29 bits)
+// rounded to nearest FP32, so |x - (h + l)| <= 2^-48 |x|.  |x| < 2^-126 gives (0, 0) and
+// 2^-126 <= |x| < 2^-74 gives l = 0 (absolute error below 2^-97); |x| >= 2^128 and
+// non-finite x give a NaN h.
+__device__ __forceinline__ void d2ff_bits(double x, float& h, float& l) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    const unsigned s = hi & 0x80000000u;
+    // h: sign | (e - 896) << 23 | top 23 mantissa bits (20 from hi, 3 from lo)
+    const unsigned hb = s | ((((hi & 0x7fffffffu) - (896u << 20)) << 3) & 0x7fffffffu) | (lo >> 29);
+    // l: the low 29 mantissa bits as an integer r, times 2^(e - 1075); r is converted exactly in
+    // two 23-bit halves through the 2^23 magic-number trick, the final fma rounds once
+    const unsigned r = lo & 0x1fffffffu;
+    const float rh = __fadd_rn(__uint_as_float(0x4b000000u | (r >> 6)), -8388608.0f);
+    const float rl = __fadd_rn(__uint_as_float(0x4b000000u | (r & 63u)), -8388608.0f);
+    const float rf = __fmaf_rn(rh, 64.0f, rl);
+    const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1075), valid for e in [949, 1202]
+    const float lf = __uint_as_float(__float_as_uint(__fmul_rn(rf, scale)) | s);
+    if (e < 897u) { h = __uint_as_float(s); l = __uint_as_float(s); }
+    else if (e > 1150u) { h = __uint_as_float(0x7fc00000u); l = 0.f; }
+    else { h = __uint_as_float(hb); l = e < 949u ? __uint_as_float(s) : lf; }
+}
+__device__ __forceinline__ float d2f_bits(double x) {  // truncation to FP32 (same range rules)
+    float h, l;
+    d2ff_bits(x, h, l);
+    return h;
+}
