@@ -136,6 +136,7 @@ struct SweepArgs {
     BSum* bsum[2];      // per chunk id, by sweep parity
     long plane;         // cells per plane (all tubes)
     int sweep, B;
+    int chunk0;         // first chunk of the launch (chunks are grouped by scheme variant)
     int* flag;
     int* item_flags;    // per tube (may be null)
 };
@@ -152,6 +153,7 @@ struct Smem1 {
     alignas(16) float sfm[2][3][MW];
     float wall[2][3][2];                // constant wall terms (order 1) for cell 0 / n-1
     double corr[2][3];                  // boundary corrections of cells a and b (previous sweep)
+    float rec[2][MW / 16][3][2];        // per-step terms at the chunk's boundary interfaces
 };
 
 // lane q of a float2
@@ -187,7 +189,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     const double lam = tp.lam;
     const float lamh = (float)lam, laml = (float)(lam - (double)lamh);
 
-    if (L > MW) {  // host guarantees this never happens; refuse rather than overrun
+    if (L > MW || A.B > MW / 16) {  // host guarantees this never happens; refuse rather than overrun
         if (tid == 0) atomicOr(A.flag, SHLL_FLAG_BADARG);
         return;
     }
@@ -281,29 +283,48 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     }
     const Coef2 c2 = coef2(fr.c);
     const float2 lamh2 = f2(lamh), laml2 = f2(laml);
-    // flux sums at the chunk's two boundary interfaces (kept by the threads that apply them)
-    float bh[2][3] = {{0, 0, 0}, {0, 0, 0}}, bl[2][3] = {{0, 0, 0}, {0, 0, 0}};
     const bool hasL = ch.idL >= 0, hasR = ch.idR >= 0;
     // loop-invariant roles of this thread's cells (i = tube cell of window cell w)
-    auto edge = [&](int w) { const int i = ws + w; return i == 0 || i == n - 1; };
-    // half-slope factors: 0.5, or 0 on edge cells (the reference's zero slopes there)
+    auto edge = [&](int w) { const int i = ws + w; return i <= 0 || i >= n - 1; };
+    // half-slope factors: 0.5, or 0 on edge cells (the reference's zero slopes there) and on the
+    // ghost cells beyond the walls
     const float2 hp = make_float2(edge(w0) ? 0.f : 0.5f, edge(w0 + 1) ? 0.f : 0.5f);
     const float2 nhm = neg2(hp);
     const float hpl = edge(w0 - 1) ? 0.f : 0.5f;    // cell w0 - 1 (sp only)
     const float nhmr = edge(w0 + 2) ? -0.f : -0.5f; // cell w0 + 2 (sm only)
-    // interface masks: a cell's left / right interface is applied unless it is a wall (the wall
-    // term replaces it) or lies outside the window
-    auto in_ok = [&](int w) { const int i = ws + w; return i > 0 && w > 0 && w < L; };
-    auto out_ok = [&](int w) { const int i = ws + w; return i < n - 1 && w < L - 1; };
+    // Second order (outflow walls, base-c/2nd_order_base_shll.c:236-262): the wall flux is the
+    // cell's own flux fp + fm, i.e. the regular interface formula with a ghost cell that copies
+    // the wall cell (fp_{-1} = fp_0, fm_n = fm_{n-1}, zero slopes), so walls need no special
+    // path.  The ghost values are substituted by selects in the wall threads.
+    const bool gl = ORDER == 2 && ws + w0 == 0;            // lane x is cell 0
+    const bool grx = ORDER == 2 && ws + w0 == n - 1;       // lane x is cell n-1
+    const bool gry = ORDER == 2 && ws + w0 + 1 == n - 1;   // lane y is cell n-1
+    // interface masks: a cell's left / right interface is applied unless it lies outside the
+    // window or (first order) is a reflective wall, whose flux the wall terms supply
+    auto in_ok = [&](int w) {
+        const int i = ws + w;
+        if (w >= L) return false;
+        return ORDER == 2 ? (w > 0 || i == 0) : (i > 0 && w > 0);
+    };
+    auto out_ok = [&](int w) {
+        const int i = ws + w;
+        if (w >= L) return false;
+        return ORDER == 2 ? (w < L - 1 || i == n - 1) : (i < n - 1 && w < L - 1);
+    };
     const float2 inm = make_float2(in_ok(w0) ? 1.f : 0.f, in_ok(w0 + 1) ? 1.f : 0.f);
     const float2 outm = make_float2(out_ok(w0) ? 1.f : 0.f, out_ok(w0 + 1) ? 1.f : 0.f);
-    bool special[2];
+    // first-order reflective walls: lane q is cell 0 or n-1 (a few threads)
+    bool wallq[2];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
         const int w = w0 + q, i = ws + w;
-        special[q] = w < L && (i == 0 || i == n - 1 || (w == pa && hasL) || (w == pb - 1 && hasR));
+        wallq[q] = ORDER == 1 && w < L && (i == 0 || i == n - 1);
     }
-    const bool any_special = special[0] || special[1];
+    const bool any_wall = wallq[0] || wallq[1];
+    // chunk-boundary records: the terms applied at interface a-1/2 (cell a's left) and b-1/2
+    // (cell b-1's right) are stored per step and summed at the end of the sweep
+    const bool rin0 = hasL && w0 == pa, rin1 = hasL && w0 + 1 == pa;
+    const bool rout0 = hasR && w0 == pb - 1, rout1 = hasR && w0 + 1 == pb - 1;
     const int jl = max(w0 - 2, 0), jr = min(w0 + 2, MW - 2);  // neighbour pairs (clamped)
 
     for (int s = 0; s < steps; s++) {
@@ -318,6 +339,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
+            if (grx) fm[k].y = fm[k].x;  // ghost fm_n of the right wall (lane y holds no cell)
             *reinterpret_cast<float2*>(&S.sfp[b][k][w0]) = fp[k];
             *reinterpret_cast<float2*>(&S.sfm[b][k][w0]) = fm[k];
         }
@@ -334,18 +356,20 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             } else {
                 const float2 pR = *reinterpret_cast<const float2*>(&S.sfp[b][k][jr]);  // fp_{w0+2}
                 const float2 mL = *reinterpret_cast<const float2*>(&S.sfm[b][k][jl]);  // fm_{w0-1}
+                const float fpl = gl ? fp[k].x : pL.y;    // fp_{w0-1} (ghost of the left wall)
+                const float fmr = gry ? fm[k].y : mR.x;   // fm_{w0+2} (ghost of the right wall)
                 // differences f_j - f_{j-1}
-                const float2 dpo = sub2(fp[k], make_float2(pL.y, fp[k].x));     // j = w0, w0+1
+                const float2 dpo = sub2(fp[k], make_float2(fpl, fp[k].x));      // j = w0, w0+1
                 const float2 dpr = sub2(make_float2(fp[k].y, pR.x), fp[k]);     // j = w0+1, w0+2
-                const float dpl = __fadd_rn(pL.y, -pL.x);                        // j = w0-1
+                const float dpl = __fadd_rn(fpl, -pL.x);                         // j = w0-1
                 const float2 dmo = sub2(fm[k], make_float2(mL.y, fm[k].x));
-                const float2 dmr = sub2(make_float2(fm[k].y, mR.x), fm[k]);
-                const float dmrr = __fadd_rn(mR.y, -mR.x);                       // j = w0+3
+                const float2 dmr = sub2(make_float2(fm[k].y, fmr), fm[k]);
+                const float dmrr = __fadd_rn(mR.y, -fmr);                        // j = w0+3
                 // reconstructed left states L_j = fp_j + sp_j/2 and right states R_j = fm_j - sm_j/2
                 const float2 Lo = fma2(hp, slope2<LIM>(dpo, dpr, tp.alpha), fp[k]);           // j = w0, w0+1
-                const float Ll = __fmaf_rn(hpl, slope_s<LIM>(dpl, dpo.x, tp.alpha), pL.y);      // j = w0-1
+                const float Ll = __fmaf_rn(hpl, slope_s<LIM>(dpl, dpo.x, tp.alpha), fpl);       // j = w0-1
                 const float2 Ro = fma2(nhm, slope2<LIM>(dmo, dmr, tp.alpha), fm[k]);          // j = w0, w0+1
-                const float Rr = __fmaf_rn(nhmr, slope_s<LIM>(dmr.y, dmrr, tp.alpha), mR.x);    // j = w0+2
+                const float Rr = __fmaf_rn(nhmr, slope_s<LIM>(dmr.y, dmrr, tp.alpha), fmr);     // j = w0+2
                 IN = add2(make_float2(Ll, Lo.x), Ro);
                 OUT = add2(Lo, make_float2(Ro.y, Rr));
             }
@@ -362,31 +386,27 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                 il = mul2(il, inm); ol = mul2(ol, outm);
                 dl[k] = add2(dl[k], sub2(il, ol));
             }
-            if (any_special) {
+            if (rin0) { S.rec[0][s][k][0] = ih.x; S.rec[0][s][k][1] = il.x; }
+            if (rin1) { S.rec[0][s][k][0] = ih.y; S.rec[0][s][k][1] = il.y; }
+            if (rout0) { S.rec[1][s][k][0] = oh.x; S.rec[1][s][k][1] = ol.x; }
+            if (rout1) { S.rec[1][s][k][0] = oh.y; S.rec[1][s][k][1] = ol.y; }
+        }
+        // ---- first-order reflective walls (the threads of cells 0 and n-1) ----
+        if (ORDER == 1 && any_wall) {
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    if (!special[q]) continue;
-                    const int w = w0 + q, i = ws + w;
+            for (int q = 0; q < 2; q++) {
+                if (!wallq[q]) continue;
+                const int i = ws + w0 + q;
+                const int bnd = i == 0 ? 0 : 1;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
                     float h = lane(dh[k], q), l = lane(dl[k], q);
-                    if (w == pa && hasL) { two_sum_acc(bh[0][k], bl[0][k], lane(ih, q)); bl[0][k] = __fadd_rn(bl[0][k], lane(il, q)); }
-                    if (w == pb - 1 && hasR) { two_sum_acc(bh[1][k], bl[1][k], lane(oh, q)); bl[1][k] = __fadd_rn(bl[1][k], lane(ol, q)); }
-                    if (i == 0 || i == n - 1) {
-                        if (ORDER == 1) {
-                            const int bnd = i == 0 ? 0 : 1;
-                            two_sum_acc(h, l, S.wall[bnd][k][0]); l = __fadd_rn(l, S.wall[bnd][k][1]);
-                            if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
-                                const float v = i == 0 ? __fmul_rn(2.f, lane(fm[1], q)) : -__fmul_rn(2.f, lane(fp[1], q));
-                                const float vh = __fmul_rn(lamh, v);
-                                const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
-                                two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
-                            }
-                        } else {  // outflow: F_{-1/2} = Fref + dfp_0 + dfm_0 (and likewise at n-1)
-                            float v = __fadd_rn(lane(fp[k], q), lane(fm[k], q));
-                            if (i == n - 1) v = -v;
-                            const float vh = __fmul_rn(lamh, v);
-                            const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
-                            two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
-                        }
+                    two_sum_acc(h, l, S.wall[bnd][k][0]); l = __fadd_rn(l, S.wall[bnd][k][1]);
+                    if (k == 1) {  // +2 lam dfm1_0 at the left wall, -2 lam dfp1_{n-1} at the right
+                        const float v = i == 0 ? __fmul_rn(2.f, lane(fm[1], q)) : -__fmul_rn(2.f, lane(fp[1], q));
+                        const float vh = __fmul_rn(lamh, v);
+                        const float vl = __fadd_rn(__fmaf_rn(lamh, v, -vh), __fmul_rn(laml, v));
+                        two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
                     }
                     set_lane(dh[k], q, h);
                     set_lane(dl[k], q, l);
@@ -395,14 +415,17 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         }
     }
     // ---- boundary flux sums of this sweep (full flux: steps * lam * Fref + sum lam*Delta) ----
-    BSum* bout = ((A.sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-        const int w = w0 + q;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            if (w == pa && hasL) bout->s[0][k] = steps * lam * fr.F[k] + (f2d_bits(bh[0][k]) + f2d_bits(bl[0][k]));
-            if (w == pb - 1 && hasR) bout->s[1][k] = steps * lam * fr.F[k] + (f2d_bits(bh[1][k]) + f2d_bits(bl[1][k]));
+    __syncthreads();
+    if (tid < 6) {
+        const int side = tid / 3, k = tid % 3;
+        if (side == 0 ? hasL : hasR) {
+            float h = 0.f, l = 0.f;
+            for (int st = 0; st < steps; st++) {
+                two_sum_acc(h, l, S.rec[side][st][k][0]);
+                l = __fadd_rn(l, S.rec[side][st][k][1]);
+            }
+            BSum* bout = ((A.sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
+            bout->s[side][k] = steps * lam * fr.F[k] + (f2d_bits(h) + f2d_bits(l));
         }
     }
 
@@ -439,23 +462,89 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     }
 }
 
-template <bool KAHAN>
+// One specialised kernel per scheme variant keeps each kernel's code small (the step loop is
+// latency-bound with few warps per SM, so instruction-fetch bubbles show directly).
+// Consecutive sweeps are chained by programmatic dependent launch: a sweep lets the next one
+// launch at once (griddepcontrol.launch_dependents); the next sweep's blocks become resident
+// beside it, read their descriptors (constant during a run) and wait in griddepcontrol.wait
+// until this grid has completed and its memory is visible (a hardware dependency, no polling).
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
 __global__ void __launch_bounds__(MT) k_sweep1d(SweepArgs A) {
     __shared__ Smem1 S;
-    const Chunk ch = A.chunks[blockIdx.x];
+    const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];
-    const bool pow2 = tp.lam_pow2;
-    if (tp.order == 2) {
-        if (tp.limiter == 1) {
-            if (pow2) sweep_chunk<2, KAHAN, true, 1>(A, ch, tp, S);
-            else sweep_chunk<2, KAHAN, false, 1>(A, ch, tp, S);
-        } else {
-            if (pow2) sweep_chunk<2, KAHAN, true, 0>(A, ch, tp, S);
-            else sweep_chunk<2, KAHAN, false, 0>(A, ch, tp, S);
-        }
-    } else {
-        if (pow2) sweep_chunk<1, KAHAN, true, 0>(A, ch, tp, S);
-        else sweep_chunk<1, KAHAN, false, 0>(A, ch, tp, S);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM>(A, ch, tp, S);
+}
+
+// scheme variant of a tube: 0/1 first order (lam a power of two or not), 2/3 second order
+// minmod, 4/5 second order MC limiter
+static int tube_variant(const TubeP& tp) {
+    if (tp.order == 1) return tp.lam_pow2 ? 0 : 1;
+    return 2 + (tp.limiter == 1 ? 2 : 0) + (tp.lam_pow2 ? 0 : 1);
+}
+
+// multiprocessors of the current device (cached per device)
+static int device_sms() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (cache[dev] == 0) {
+        int v = 1;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = v > 0 ? v : 1;
+    }
+    return cache[dev];
+}
+
+// Dynamic shared memory that keeps a sweep block alone on its SM.  For a grid of at most one
+// block per SM the next sweep's blocks (launched early, see k_sweep1d) could otherwise be packed
+// two or three to an SM while others stay empty; with this padding each one waits for an SM of
+// its own.  Grids of several waves launch without it.
+constexpr int kSoloSmem = 120 * 1024;
+
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
+static cudaError_t launch_one(int grid, cudaStream_t s, const SweepArgs& A, bool pdl) {
+    static unsigned long long attr_set = 0;  // devices on which the padding is allowed
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool solo = pdl && grid <= device_sms();
+    if (solo && dev < 64 && !(attr_set & (1ull << dev))) {
+        cudaError_t e = cudaFuncSetAttribute(k_sweep1d<ORDER, KAHAN, LAM_POW2, LIM>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, kSoloSmem);
+        if (e != cudaSuccess) return e;
+        attr_set |= 1ull << dev;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(MT);
+    cfg.dynamicSmemBytes = solo ? kSoloSmem : 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_sweep1d<ORDER, KAHAN, LAM_POW2, LIM>, A);
+}
+
+// pdl: chain to the previous sweep of the same run (the first sweep of a run follows the
+// descriptor uploads with ordinary stream order)
+static cudaError_t launch_sweep(int variant, bool kahan, int grid, cudaStream_t s, const SweepArgs& A, bool pdl) {
+    switch (variant * 2 + (kahan ? 1 : 0)) {
+        case 0: return launch_one<1, false, true, 0>(grid, s, A, pdl);
+        case 1: return launch_one<1, true, true, 0>(grid, s, A, pdl);
+        case 2: return launch_one<1, false, false, 0>(grid, s, A, pdl);
+        case 3: return launch_one<1, true, false, 0>(grid, s, A, pdl);
+        case 4: return launch_one<2, false, true, 0>(grid, s, A, pdl);
+        case 5: return launch_one<2, true, true, 0>(grid, s, A, pdl);
+        case 6: return launch_one<2, false, false, 0>(grid, s, A, pdl);
+        case 7: return launch_one<2, true, false, 0>(grid, s, A, pdl);
+        case 8: return launch_one<2, false, true, 1>(grid, s, A, pdl);
+        case 9: return launch_one<2, true, true, 1>(grid, s, A, pdl);
+        case 10: return launch_one<2, false, false, 1>(grid, s, A, pdl);
+        default: return launch_one<2, true, false, 1>(grid, s, A, pdl);
     }
 }
 
@@ -774,9 +863,12 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
         maxsteps = std::max(maxsteps, steps[t]);
     }
     if (maxsteps == 0) return SHLL_OK;
-    // chunks ordered by their tube's sweep count, so launch k covers a prefix of the list
+    // chunks grouped by scheme variant and, inside a group, ordered by their tube's sweep count,
+    // so that the launch of sweep k for a group covers a prefix of the group
     std::vector<Chunk> order = m->chunks;
     std::stable_sort(order.begin(), order.end(), [&](const Chunk& x, const Chunk& y) {
+        const int vx = tube_variant(m->tubes[x.tube]), vy = tube_variant(m->tubes[y.tube]);
+        if (vx != vy) return vx < vy;
         return m->tubes[x.tube].steps > m->tubes[y.tube].steps;
     });
     if (cudaMemcpyAsync(m->d_tubes, m->tubes.data(), sizeof(TubeP) * m->nitems, cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
@@ -785,12 +877,17 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
         return SHLL_ERR_CUDA;
     }
     const long nsweeps = (maxsteps + m->B - 1) / m->B;
-    // active[k] = chunks whose tube still has sweep k (suffix sum of a histogram of sweep counts)
-    std::vector<int> active(nsweeps + 1, 0);
-    for (const Chunk& c : order) active[(m->tubes[c.tube].steps + m->B - 1) / m->B]++;
-    for (long k = nsweeps - 1; k >= 0; k--) active[k] += active[k + 1];
-    std::vector<int> launch(nsweeps);
-    for (long k = 0; k < nsweeps; k++) launch[k] = active[k + 1];
+    struct Group { int variant, first; std::vector<int> active; };
+    std::vector<Group> groups;
+    for (int c = 0; c < (int)order.size(); c++) {
+        const TubeP& tp = m->tubes[order[c].tube];
+        const int v = tube_variant(tp);
+        if (groups.empty() || groups.back().variant != v) groups.push_back({v, c, std::vector<int>(nsweeps + 1, 0)});
+        // active[k] = chunks of the group whose tube still has sweep k (suffix sum of a histogram)
+        groups.back().active[(tp.steps + m->B - 1) / m->B]++;
+    }
+    for (Group& g : groups)
+        for (long k = nsweeps - 1; k >= 0; k--) g.active[k] += g.active[k + 1];
     SweepArgs A;
     A.tubes = m->d_tubes;
     A.chunks = m->d_chunks;
@@ -802,13 +899,22 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     A.flag = m->d_flag;
     A.item_flags = m->d_item_flags;
     A.sweep = 0;
-    shll_count_launches(nsweeps + 1);
-    for (long k = 0; k < nsweeps; k++) {
+    long launches = 1;  // + the fix-up
+    cudaError_t le = cudaSuccess;
+    for (long k = 0; k < nsweeps && le == cudaSuccess; k++) {
         A.sweep = (int)k;
-        if (launch[k] == 0) continue;
-        if (m->kahan) k_sweep1d<true><<<launch[k], MT, 0, m->stream>>>(A);
-        else k_sweep1d<false><<<launch[k], MT, 0, m->stream>>>(A);
+        for (const Group& g : groups) {
+            const int cnt = g.active[k + 1];
+            if (cnt == 0) continue;
+            A.chunk0 = g.first;
+            le = launch_sweep(g.variant, m->kahan, cnt, m->stream, A, launches > 1);
+            if (le != cudaSuccess) break;
+            launches++;
+        }
     }
+    if (le != cudaSuccess) { snprintf(err, len, "sweep launch failed: %s", cudaGetErrorString(le)); return SHLL_ERR_CUDA; }
+    shll_count_launches(launches);
+    A.chunk0 = 0;
     const int nch = (int)order.size();
     if (m->kahan) k_fixup1d<true><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);
     else k_fixup1d<false><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);
@@ -1081,11 +1187,16 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.B = B;
     A.flag = d_flag;
     A.item_flags = nullptr;
+    A.chunk0 = 0;
     const long nsweeps = (nsteps + B - 1) / B;
     shll_count_launches(nsweeps + 1);
-    for (long w = 0; w < nsweeps; w++) {
+    for (long w = 0; w < nsweeps && e == cudaSuccess; w++) {
         A.sweep = (int)w;
-        k_sweep1d<false><<<k, MT, 0, s>>>(A);
+        e = launch_sweep(tube_variant(tp), false, k, s, A, w > 0);
+    }
+    if (e != cudaSuccess) {
+        fprintf(stderr, "shll_tube_run_static: sweep launch failed: %s\n", cudaGetErrorString(e));
+        return SHLL_ERR_CUDA;
     }
     k_fixup1d<false><<<(k + 127) / 128, 128, 0, s>>>(A, k);
     e = cudaGetLastError();
