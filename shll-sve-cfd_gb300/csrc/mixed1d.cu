@@ -325,6 +325,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     // (cell b-1's right) are stored per step and summed at the end of the sweep
     const bool rin0 = hasL && w0 == pa, rin1 = hasL && w0 + 1 == pa;
     const bool rout0 = hasR && w0 == pb - 1, rout1 = hasR && w0 + 1 == pb - 1;
+    const bool any_rec = rin0 || rin1 || rout0 || rout1;
     const int jl = max(w0 - 2, 0), jr = min(w0 + 2, MW - 2);  // neighbour pairs (clamped)
 
     for (int s = 0; s < steps; s++) {
@@ -345,6 +346,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         }
         __syncthreads();
         // ---- interfaces w0-1/2 (IN.x), w0+1/2 (IN.y = OUT.x), w0+3/2 (OUT.y) ----
+        float2 ihk[3], ohk[3], ilk[3], olk[3];  // applied terms (for the boundary records)
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const float2 pL = *reinterpret_cast<const float2*>(&S.sfp[b][k][jl]);  // fp_{w0-2}, fp_{w0-1}
@@ -386,10 +388,16 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                 il = mul2(il, inm); ol = mul2(ol, outm);
                 dl[k] = add2(dl[k], sub2(il, ol));
             }
-            if (rin0) { S.rec[0][s][k][0] = ih.x; S.rec[0][s][k][1] = il.x; }
-            if (rin1) { S.rec[0][s][k][0] = ih.y; S.rec[0][s][k][1] = il.y; }
-            if (rout0) { S.rec[1][s][k][0] = oh.x; S.rec[1][s][k][1] = ol.x; }
-            if (rout1) { S.rec[1][s][k][0] = oh.y; S.rec[1][s][k][1] = ol.y; }
+            ihk[k] = ih; ohk[k] = oh; ilk[k] = il; olk[k] = ol;
+        }
+        if (any_rec) {  // the threads of cells a and b-1 (warp-uniform elsewhere)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (rin0) { S.rec[0][s][k][0] = ihk[k].x; S.rec[0][s][k][1] = ilk[k].x; }
+                if (rin1) { S.rec[0][s][k][0] = ihk[k].y; S.rec[0][s][k][1] = ilk[k].y; }
+                if (rout0) { S.rec[1][s][k][0] = ohk[k].x; S.rec[1][s][k][1] = olk[k].x; }
+                if (rout1) { S.rec[1][s][k][0] = ohk[k].y; S.rec[1][s][k][1] = olk[k].y; }
+            }
         }
         // ---- first-order reflective walls (the threads of cells 0 and n-1) ----
         if (ORDER == 1 && any_wall) {
@@ -469,7 +477,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
 // beside it, read their descriptors (constant during a run) and wait in griddepcontrol.wait
 // until this grid has completed and its memory is visible (a hardware dependency, no polling).
 template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
-__global__ void __launch_bounds__(MT) k_sweep1d(SweepArgs A) {
+__global__ void __launch_bounds__(MT, 3) k_sweep1d(SweepArgs A) {
     __shared__ Smem1 S;
     const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];

@@ -123,15 +123,19 @@ __device__ __forceinline__ void two_sum_acc2(float2& h, float2& l, float2 v) {
     l = add2(l, e);
 }
 
-// minmod(a, b) = max(min(a,b),0) + min(max(a,b),0): the smaller magnitude when a and b have
-// the same sign, else 0 (one of the two terms is always 0, so the sum is exact); symmetric in
-// a and b, so every thread that evaluates the same slope gets the same bits
+// minmod(a, b): the smaller magnitude with the common sign when a and b have the same sign,
+// else 0.  Three integer/min-max operations: t = min(|a|,|b|) carrying sign(a) xor sign(b)
+// (PTX min.xorsign.abs), r = max(t, 0) (0 unless the signs agree), then sign(a) on r.
+// Symmetric in a and b up to the sign of a zero result, so threads that evaluate the same slope
+// get the same value.
 __device__ __forceinline__ float minmod_s(float a, float b) {
-    return __fadd_rn(fmaxf(fminf(a, b), 0.f), fminf(fmaxf(a, b), 0.f));
+    float t;
+    asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(t) : "f"(a), "f"(b));
+    const float r = fmaxf(t, 0.f);
+    return __uint_as_float(__float_as_uint(r) | (__float_as_uint(a) & 0x80000000u));
 }
 __device__ __forceinline__ float2 minmod2(float2 a, float2 b) {
-    return add2(make_float2(fmaxf(fminf(a.x, b.x), 0.f), fmaxf(fminf(a.y, b.y), 0.f)),
-                make_float2(fminf(fmaxf(a.x, b.x), 0.f), fminf(fmaxf(a.y, b.y), 0.f)));
+    return make_float2(minmod_s(a.x, b.x), minmod_s(a.y, b.y));
 }
 // limited slope from the backward and forward differences a = f_j - f_{j-1}, b = f_{j+1} - f_j:
 // minmod (LIM = 0) or the MC limiter minmod((a+b)/2, alpha minmod(a,b)) (LIM = 1,
