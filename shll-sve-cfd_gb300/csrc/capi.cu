@@ -326,10 +326,16 @@ extern "C" int shll_set_stream(shll_ctx* c, void* s) {
     return SHLL_OK;
 }
 
+// reads the error flag of the context's engine (the plain kernels' flag, or the mixed engine's)
 static int check_flag(shll_ctx* c) {
     int h = 0;
-    CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (c->plain) {
+        CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    } else {
+        h = mixed_flags(c->mixed);
+        CUDA_TRY(c, cudaGetLastError());
+    }
     if (h & SHLL_FLAG_TIMEOUT) { set_err(c, "a bounded device wait expired"); return SHLL_ERR_TIMEOUT; }
     if (h & SHLL_FLAG_BADARG) { set_err(c, "a kernel rejected its launch arguments"); return SHLL_ERR_ARG; }
     if (h & SHLL_FLAG_NONPOSITIVE) { set_err(c, "non-positive or NaN density/temperature reached"); return SHLL_ERR_NUMERIC; }

@@ -446,10 +446,12 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         const int w = w0 + q;
         if (w < pa || w >= pb) continue;
         float uf[3];
+        bool finite = true;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const long idx = k * P + base + ws + w;
             const float h = lane(dh[k], q), l = lane(dl[k], q);
+            finite = finite && isfinite(h) && isfinite(l);
             if (KAHAN) {
                 float oh, ol;
                 ff_add(fr.Uh[k], fr.Ul[k], h, l, oh, ol);
@@ -462,7 +464,8 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             }
         }
         const float eint = __fadd_rn(uf[2], -__fmul_rn(0.5f, __fdividef(__fmul_rn(uf[1], uf[1]), uf[0])));
-        bad |= !(uf[0] > 0.f) || !(eint > 0.f);
+        // breakdown: non-positive density or internal energy, or an overflowed / NaN increment
+        bad |= !(uf[0] > 0.f) || !(eint > 0.f) || !finite;
     }
     if (bad) {
         atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);

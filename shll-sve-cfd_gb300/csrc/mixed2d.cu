@@ -276,7 +276,8 @@ __global__ void __launch_bounds__(NT) k_fold2d(Args2 A) {
                 U[k] = v;
             }
         }
-        bad = !(U[0] > 0.0) || !(U[3] > 0.0);
+        // breakdown: non-positive density or energy, or a non-finite state
+        bad = !(U[0] > 0.0) || !(U[3] > 0.0) || !isfinite(U[0] + U[1] + U[2] + U[3]);
         if (li == hi_i / 2 && lj == hi_j / 2)
             for (int k = 0; k < 4; k++) sU[k] = U[k];
     }

@@ -92,3 +92,16 @@ def test_batch_matches_single_contexts_and_oracle(shll, oracle):
         single.run()
         assert np.array_equal(single.primitives(), out)
     assert b.cell_updates == sum(p.nx * shll.steps_for(p) for p in items)
+
+
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+def test_single_tube_breakdown_is_reported(shll, oracle, prec):
+    # The reference's second-order scheme breaks down (NaN) on this tube; a single-context run of
+    # the mixed engine must report it (SHLL_ERR_NUMERIC) rather than return a NaN state silently.
+    ref = oracle.run(oracle.make_cfg(order=2, nx=512), oracle.ic_sod(512, rhoL=100.0, TL=2.0))[1]
+    assert np.isnan(ref).any()
+    c = shll.Context(shll.params(1, 2, nx=512, precision=prec, ic_rho_l=100.0, ic_T_l=2.0))
+    c.init_state()
+    with pytest.raises(shll.ShllError) as e:
+        c.run()
+    assert e.value.status == shll.ERR_NUMERIC
