@@ -40,6 +40,8 @@ namespace {
 
 constexpr int MW = 512;       // window capacity (cells) of one CTA
 constexpr int MT = MW / 2;    // threads per CTA: two adjacent cells per thread (FP32x2 lanes)
+constexpr int kSweepSteps = 16;      // steps per sweep (temporal blocking depth)
+constexpr int kDefaultFold1D = 64;   // default FP64 fold interval (steps)
 
 struct TubeP {
     long base;        // offset of cell 0 in the planes
@@ -51,6 +53,7 @@ struct TubeP {
     float alpha;
     float gRf, Rf, cvinvf;  // gamma R, R, 1/CV in FP32
     int lam_pow2;     // lam is a power of two: lam*Delta is exact in FP32
+    int fold_sweeps;  // sweeps per fold window (FP64 state read at the first, written at the last)
 };
 
 struct Chunk {
@@ -134,6 +137,9 @@ struct SweepArgs {
     void* hi[2];        // state planes of each buffer (double, or FP32 value)
     float* lo[2];       // FP32 compensation planes (Kahan)
     BSum* bsum[2];      // per chunk id, by sweep parity
+    float* dh[2];       // deviation pairs between the sweeps of a fold window (value, compensation)
+    float* dl[2];
+    Frame1* frames;     // per chunk id: the frame of the current fold window
     long plane;         // cells per plane (all tubes)
     int sweep, B;
     int chunk0;         // first chunk of the launch (chunks are grouped by scheme variant)
@@ -152,9 +158,12 @@ struct Smem1 {
     alignas(16) float sfp[2][3][MW];    // split-flux deviations, double-buffered by step parity
     alignas(16) float sfm[2][3][MW];
     float wall[2][3][2];                // constant wall terms (order 1) for cell 0 / n-1
-    double corr[2][3];                  // boundary corrections of cells a and b (previous sweep)
+    float corrp[2][3][2];               // boundary corrections of cells a and b (previous sweep), FP32 pairs
+    float dnb[2][3][2];                 // U*(left / right neighbour) - U*(this chunk), FP32 pairs
     float rec[2][MW / 16][3][2];        // per-step terms at the chunk's boundary interfaces
 };
+constexpr int kFrameWords = (int)(sizeof(Frame1) / 4);
+static_assert(sizeof(Frame1) % 4 == 0 && kFrameWords <= MT, "frame copy by one word per thread");
 
 // lane q of a float2
 __device__ __forceinline__ float lane(float2 v, int q) { return q ? v.y : v.x; }
@@ -181,9 +190,18 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     const int ws = max(0, ch.a - H), we = min(n, ch.b + H), L = we - ws;
     const int pa = ch.a - ws, pb = ch.b - ws;  // first owned / one past the last owned, window coords
     const int inb = (tp.par + A.sweep) & 1, outb = inb ^ 1;
+    // position in the fold window: the first sweep reads the stored state and sets the frame,
+    // the last one writes the state back; the sweeps between exchange deviation pairs
+    const int F = tp.fold_sweeps;
+    const int jw = A.sweep % F;
+    const int nsw = (tp.steps + A.B - 1) / A.B;
+    const bool wstart = jw == 0;
+    const bool wend = jw == F - 1 || A.sweep == nsw - 1;
     // (selects rather than indexing the parameter arrays, which would copy them to local memory)
     const void* hin = inb ? A.hi[1] : A.hi[0];
     const float* lin = inb ? A.lo[1] : A.lo[0];
+    const float* dhin = inb ? A.dh[1] : A.dh[0];
+    const float* dlin = inb ? A.dl[1] : A.dl[0];
     const long base = tp.base;
     const long P = A.plane;
     const double lam = tp.lam;
@@ -195,8 +213,8 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     }
     // the window's stored values, loaded first so that their latency overlaps the frame setup
     const int w0 = 2 * tid;
-    double uin[2][3];           // FP64 state
-    float uh[2][3], ul[2][3];   // FP32 value + compensation (KAHAN)
+    double uin[2][3];           // FP64 state (window start)
+    float uh[2][3], ul[2][3];   // FP32 value + compensation (KAHAN window start), or deviation pair
 #pragma unroll
     for (int q = 0; q < 2; q++)
 #pragma unroll
@@ -205,51 +223,68 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             const int w = w0 + q;
             if (w < L) {
                 const long idx = k * P + base + ws + w;
-                if (KAHAN) { uh[q][k] = static_cast<const float*>(hin)[idx]; ul[q][k] = lin[idx]; }
+                if (!wstart) { uh[q][k] = dhin[idx]; ul[q][k] = dlin[idx]; }
+                else if (KAHAN) { uh[q][k] = static_cast<const float*>(hin)[idx]; ul[q][k] = lin[idx]; }
                 else uin[q][k] = static_cast<const double*>(hin)[idx];
             }
         }
-    double Uanc[3];
-    float Uanc_h[3], Uanc_l[3];
-    if (tid == 0)
-        for (int k = 0; k < 3; k++) {
-            const long idx = k * P + base + ch.anc;
-            if (KAHAN) { Uanc_h[k] = static_cast<const float*>(hin)[idx]; Uanc_l[k] = lin[idx]; }
-            else Uanc[k] = static_cast<const double*>(hin)[idx];
+    // correction of the previous sweep owed to cell a (side 0, by the left neighbour) or to cell b
+    // (side 1: the right neighbour's first cell, which lies in this window's halo)
+    auto corr_of = [&](int side, int k) -> double {
+        if (A.sweep == 0) return 0.0;
+        const BSum* bs = ((A.sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
+        if (side == 0) return ch.idL >= 0 ? boundary_correction(bs, ch.idL, ch.id, k) : 0.0;
+        return ch.idR >= 0 ? boundary_correction(bs, ch.id, ch.idR, k) : 0.0;
+    };
+    // The frame: computed from the anchor cell at the start of a fold window (one thread, then a
+    // barrier), read from the per-chunk table by the other sweeps of the window
+    const Frame1* frp = wstart ? &fr : &A.frames[ch.id];
+    // corrections and (inside a window) neighbour-frame offsets as FP32 pairs, once per block
+    if (tid < 12 && (tid < 6 || !wstart)) {
+        const int side = (tid % 6) / 3, k = tid % 3;
+        double v;
+        if (tid < 6) {
+            v = corr_of(side, k);
+        } else {
+            const int nb = side == 0 ? ch.idL : ch.idR;
+            v = nb >= 0 ? A.frames[nb].U[k] - frp->U[k] : 0.0;
         }
-    // corrections of the previous sweep for cell a (from the left neighbour) and cell b (the right
-    // neighbour's first cell, which lies in this window's halo)
-    if (tid < 6) {
-        const int side = tid / 3, k = tid % 3;
-        double c = 0.0;
-        if (A.sweep > 0) {
-            const BSum* bs = ((A.sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
-            if (side == 0 && ch.idL >= 0) c = boundary_correction(bs, ch.idL, ch.id, k);
-            if (side == 1 && ch.idR >= 0) c = boundary_correction(bs, ch.id, ch.idR, k);
+        float* o = tid < 6 ? S.corrp[side][k] : S.dnb[side][k];
+        d2ff_bits(v, o[0], o[1]);
+    }
+    if (wstart) {
+        if (tid == 0) {
+            double U[3];
+            float Uanc_h[3], Uanc_l[3];
+            const bool corrected = ch.anc == ch.a || ch.anc == ch.b;
+            for (int k = 0; k < 3; k++) {
+                const long idx = k * P + base + ch.anc;
+                if (KAHAN) {
+                    Uanc_h[k] = static_cast<const float*>(hin)[idx];
+                    Uanc_l[k] = lin[idx];
+                    U[k] = f2d_bits(Uanc_h[k]) + f2d_bits(Uanc_l[k]);
+                } else {
+                    U[k] = static_cast<const double*>(hin)[idx];
+                }
+                if (ch.anc == ch.a) U[k] += corr_of(0, k);
+                if (ch.anc == ch.b) U[k] += corr_of(1, k);
+            }
+            make_frame(fr, U, tp, ORDER == 1 && (ch.idL < 0 || ch.idR < 0));
+            if (KAHAN && !corrected)  // the stored pair itself, so that the anchor cell's deviation is exactly 0
+                for (int k = 0; k < 3; k++) { fr.Uh[k] = Uanc_h[k]; fr.Ul[k] = Uanc_l[k]; }
         }
-        S.corr[side][k] = c;
     }
     __syncthreads();
-    if (tid == 0) {
-        double U[3];
-        const bool corrected = ch.anc == ch.a || ch.anc == ch.b;
-        for (int k = 0; k < 3; k++) {
-            U[k] = KAHAN ? f2d_bits(Uanc_h[k]) + f2d_bits(Uanc_l[k]) : Uanc[k];
-            if (ch.anc == ch.a) U[k] += S.corr[0][k];
-            if (ch.anc == ch.b) U[k] += S.corr[1][k];
-        }
-        make_frame(fr, U, tp, ORDER == 1 && (ch.idL < 0 || ch.idR < 0));
-        if (KAHAN && !corrected)  // the stored pair itself, so that the anchor cell's deviation is exactly 0
-            for (int k = 0; k < 3; k++) { fr.Uh[k] = Uanc_h[k]; fr.Ul[k] = Uanc_l[k]; }
-    }
-    __syncthreads();
+    if (wstart && !wend && tid < kFrameWords)  // keep the frame for the rest of the window
+        reinterpret_cast<unsigned*>(&A.frames[ch.id])[tid] = reinterpret_cast<const unsigned*>(&fr)[tid];
     if (tid < 6 && ORDER == 1) {
-        // reflective walls: constant parts of the wall-cell increments
+        // reflective walls: constant parts of the wall-cell increments (read after the first step's
+        // barrier)
         // cell 0:   lam*F_{-1/2} - lam*Fref = (-lam F0, lam (2 fmS1 - F1), -lam F2) (+2 lam dfm1_0)
         // cell n-1: lam*Fref - lam*F_{n-1/2} = (lam F0, lam (F1 - 2 fpS1), lam F2) (-2 lam dfp1_{n-1})
         const int bnd = tid / 3, k = tid % 3;
-        double w = bnd == 0 ? (k == 1 ? lam * (2.0 * fr.fmS1 - fr.F[1]) : -lam * fr.F[k])
-                            : (k == 1 ? lam * (fr.F[1] - 2.0 * fr.fpS1) : lam * fr.F[k]);
+        double w = bnd == 0 ? (k == 1 ? lam * (2.0 * frp->fmS1 - frp->F[1]) : -lam * frp->F[k])
+                            : (k == 1 ? lam * (frp->F[1] - 2.0 * frp->fpS1) : lam * frp->F[k]);
         d2ff_bits(w, S.wall[bnd][k][0], S.wall[bnd][k][1]);
     }
 
@@ -263,25 +298,31 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             float h = 0.f, l = 0.f;
             if (w < L) {
                 const bool corrected = w == pa || w == pb;  // cells owed a boundary correction
-                if (KAHAN) {
-                    const float vh = uh[q][k], vl = ul[q][k];
+                if (!wstart) {
+                    // deviation pair relative to the owner's frame -> relative to this frame
+                    h = uh[q][k]; l = ul[q][k];
+                    if (w < pa || w >= pb) {
+                        const int sd = w < pa ? 0 : 1;
+                        ff_add(h, l, S.dnb[sd][k][0], S.dnb[sd][k][1], h, l);
+                    }
                     if (corrected) {
-                        const double d = ((f2d_bits(vh) - fr.U[k]) + f2d_bits(vl)) + S.corr[w == pa ? 0 : 1][k];
-                        d2ff_bits(d, h, l);
-                    } else {
-                        ff_sub(vh, vl, fr.Uh[k], fr.Ul[k], h, l);
+                        const int sd = w == pa ? 0 : 1;
+                        ff_add(h, l, S.corrp[sd][k][0], S.corrp[sd][k][1], h, l);
                     }
                 } else {
-                    double d = uin[q][k] - fr.U[k];
-                    if (corrected) d += S.corr[w == pa ? 0 : 1][k];
-                    d2ff_bits(d, h, l);
+                    if (KAHAN) ff_sub(uh[q][k], ul[q][k], frp->Uh[k], frp->Ul[k], h, l);
+                    else d2ff_bits(uin[q][k] - frp->U[k], h, l);
+                    if (corrected) {
+                        const int sd = w == pa ? 0 : 1;
+                        ff_add(h, l, S.corrp[sd][k][0], S.corrp[sd][k][1], h, l);
+                    }
                 }
             }
             set_lane(dh[k], q, h);
             set_lane(dl[k], q, l);
         }
     }
-    const Coef2 c2 = coef2(fr.c);
+    const Coef2 c2 = coef2(frp->c);
     const float2 lamh2 = f2(lamh), laml2 = f2(laml);
     const bool hasL = ch.idL >= 0, hasR = ch.idR >= 0;
     // loop-invariant roles of this thread's cells (i = tube cell of window cell w)
@@ -433,14 +474,17 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                 l = __fadd_rn(l, S.rec[side][st][k][1]);
             }
             BSum* bout = ((A.sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
-            bout->s[side][k] = steps * lam * fr.F[k] + (f2d_bits(h) + f2d_bits(l));
+            bout->s[side][k] = steps * lam * frp->F[k] + (f2d_bits(h) + f2d_bits(l));
         }
     }
 
-    // ---- fold the owned cells into the stored state ----
+    // ---- fold the owned cells into the stored state (last sweep of a window), or pass their
+    // deviation pairs to the next sweep ----
     int bad = 0;
     void* hout = outb ? A.hi[1] : A.hi[0];
     float* lout = outb ? A.lo[1] : A.lo[0];
+    float* dhout = outb ? A.dh[1] : A.dh[0];
+    float* dlout = outb ? A.dl[1] : A.dl[0];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
         const int w = w0 + q;
@@ -452,15 +496,19 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             const long idx = k * P + base + ws + w;
             const float h = lane(dh[k], q), l = lane(dl[k], q);
             finite = finite && isfinite(h) && isfinite(l);
-            if (KAHAN) {
+            if (!wend) {
+                dhout[idx] = h;
+                dlout[idx] = l;
+                uf[k] = __fadd_rn(frp->Uh[k], h);
+            } else if (KAHAN) {
                 float oh, ol;
-                ff_add(fr.Uh[k], fr.Ul[k], h, l, oh, ol);
+                ff_add(frp->Uh[k], frp->Ul[k], h, l, oh, ol);
                 static_cast<float*>(hout)[idx] = oh;
                 lout[idx] = ol;
                 uf[k] = oh;
             } else {
-                static_cast<double*>(hout)[idx] = fr.U[k] + (f2d_bits(h) + f2d_bits(l));
-                uf[k] = __fadd_rn(fr.Uh[k], h);  // FP32 estimate, for the positivity check only
+                static_cast<double*>(hout)[idx] = frp->U[k] + (f2d_bits(h) + f2d_bits(l));
+                uf[k] = __fadd_rn(frp->Uh[k], h);  // FP32 estimate, for the positivity check only
             }
         }
         const float eint = __fadd_rn(uf[2], -__fmul_rn(0.5f, __fdividef(__fmul_rn(uf[1], uf[1]), uf[0])));
@@ -605,6 +653,9 @@ struct MixedState {
     int* d_flag = nullptr;
     int* d_item_flags = nullptr;       // per item
     BSum* bsum[2] = {nullptr, nullptr};  // boundary flux sums per chunk id, by sweep parity
+    float* dh[2] = {nullptr, nullptr};   // deviation pairs between the sweeps of a fold window
+    float* dl[2] = {nullptr, nullptr};
+    Frame1* frames = nullptr;            // per chunk: frame of the current fold window
     long cell_updates = 0;
     // device checkpoint (shll_checkpoint)
     void* ck_hi[2] = {nullptr, nullptr};
@@ -667,6 +718,20 @@ static int alloc_mixed(MixedState* m, char* err, size_t len) {
             return SHLL_ERR_NOMEM;
         }
     }
+    bool windows = false;
+    for (const TubeP& tp : m->tubes) windows = windows || tp.fold_sweeps > 1;
+    if (windows) {
+        for (int b = 0; b < 2; b++)
+            if (cudaMalloc(&m->dh[b], cells * sizeof(float)) != cudaSuccess ||
+                cudaMalloc(&m->dl[b], cells * sizeof(float)) != cudaSuccess) {
+                snprintf(err, len, "cudaMalloc of deviation planes failed");
+                return SHLL_ERR_NOMEM;
+            }
+        if (cudaMalloc(&m->frames, sizeof(Frame1) * m->chunks.size()) != cudaSuccess) {
+            snprintf(err, len, "cudaMalloc of the frame table failed");
+            return SHLL_ERR_NOMEM;
+        }
+    }
     if (cudaMalloc(&m->d_item_flags, sizeof(int) * m->nitems) != cudaSuccess ||
         cudaMemset(m->d_item_flags, 0, sizeof(int) * m->nitems) != cudaSuccess) {
         snprintf(err, len, "cudaMalloc of item flags failed");
@@ -711,6 +776,7 @@ static TubeP tube_params(const shll_params& p, long base) {
     tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
     tp.steps = 0;
     tp.par = 0;
+    tp.fold_sweeps = 1;
     return tp;
 }
 
@@ -730,7 +796,7 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
     m->dim = items[0].dim;
     m->precision = items[0].precision;
     m->kahan = m->precision == SHLL_PREC_MIXED_KAHAN;
-    int fold = items[0].fold_steps > 0 ? items[0].fold_steps : 16;
+    const int fold = items[0].fold_steps > 0 ? items[0].fold_steps : kDefaultFold1D;
     for (int t = 0; t < count; t++) {
         if (items[t].dim != m->dim || items[t].precision != m->precision) {
             snprintf(err, len, "batch items must share dim and precision");
@@ -755,8 +821,10 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
         if (!mixed2d_attach(m, err, len)) { mixed_destroy(m); return nullptr; }
         return m;
     }
-    // sweep length: the fold interval, capped so that a chunk keeps at least half its window
-    m->B = std::min(fold, MW / 16);
+    // sweep length B (temporal blocking depth) and sweeps per fold window: the FP64 state is read
+    // and written once per fold window of (fold / B) * B steps
+    m->B = std::min(fold, kSweepSteps);
+    const int fold_sweeps = std::max(1, fold / m->B);
     long off = 0;
     for (int t = 0; t < count; t++) {
         const shll_params& p = items[t];
@@ -766,6 +834,11 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
     m->plane = off;
     m->par.assign(count, 0);
     build_chunks(m);
+    // windows of several sweeps need every halo cell to come from the adjacent chunk
+    std::vector<int> min_owned(count, 1 << 30);
+    for (const Chunk& c : m->chunks) min_owned[c.tube] = std::min(min_owned[c.tube], c.b - c.a);
+    for (int t = 0; t < count; t++)
+        m->tubes[t].fold_sweeps = min_owned[t] >= m->tubes[t].order * m->B ? fold_sweeps : 1;
     int rc = alloc_mixed(m, err, len);
     if (rc == SHLL_OK && cudaMalloc(&m->d_chunks, sizeof(Chunk) * m->chunks.size()) != cudaSuccess) rc = SHLL_ERR_NOMEM;
     if (rc != SHLL_OK) {
@@ -784,7 +857,9 @@ void mixed_destroy(MixedState* m) {
     if (m->d2) mixed2d_detach(m);
     for (int b = 0; b < 2; b++) {
         cudaFree(m->hi[b]); cudaFree(m->lo[b]); cudaFree(m->ck_hi[b]); cudaFree(m->ck_lo[b]);
+        cudaFree(m->dh[b]); cudaFree(m->dl[b]);
     }
+    cudaFree(m->frames);
     cudaFree(m->d_tubes);
     cudaFree(m->d_chunks);
     cudaFree(m->bsum[0]);
@@ -905,6 +980,9 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     A.hi[0] = m->hi[0]; A.hi[1] = m->hi[1];
     A.lo[0] = m->lo[0]; A.lo[1] = m->lo[1];
     A.bsum[0] = m->bsum[0]; A.bsum[1] = m->bsum[1];
+    A.dh[0] = m->dh[0]; A.dh[1] = m->dh[1];
+    A.dl[0] = m->dl[0]; A.dl[1] = m->dl[1];
+    A.frames = m->frames;
     A.plane = m->plane;
     A.B = m->B;
     A.flag = m->d_flag;
@@ -1157,7 +1235,7 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // descriptors of the tube, built on the stack
-    const int fold = p->fold_steps > 0 ? p->fold_steps : 16;
+    const int fold = p->fold_steps > 0 ? p->fold_steps : kSweepSteps;
     const int B = std::min(fold, MW / 16);
     TubeP tp = tube_params(*p, 0);
     tp.steps = (int)nsteps;
@@ -1192,6 +1270,8 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.hi[0] = d_cons;
     A.hi[1] = sc;  // the second state buffer
     A.lo[0] = A.lo[1] = nullptr;
+    A.dh[0] = A.dh[1] = A.dl[0] = A.dl[1] = nullptr;  // one sweep per fold window: no pairs, no frame table
+    A.frames = nullptr;
     A.bsum[0] = reinterpret_cast<BSum*>(sc + kStaticBSumOff);
     A.bsum[1] = A.bsum[0] + kStaticMaxChunks;
     A.plane = n;
