@@ -203,9 +203,29 @@ class Problem:
         self.obj = None
 
     def reset(self):
-        """Brings the initial state onto the device (untimed)."""
+        """Brings the initial state onto the device (untimed).  1D problems are built once and reset
+        by a device-side restore of the initial state (so repeated runs replay their captured launch
+        sequence); 2D problems are rebuilt."""
+        if self.obj is not None and self.dim == 1:
+            self.obj.restore()
+            return
         if self.obj is not None:
             self.obj.close()
+        if self.batch:
+            self.obj = self.shll.Batch(self.items)
+        else:
+            self.obj = self.shll.Context(self.p)
+            self.obj.init_state()
+        self.obj.set_stream(self.stream.cuda_stream)
+        if self.dim == 1:
+            self.obj.checkpoint()
+
+    def reset_from_host(self):
+        """Rebuilds the problem from host data (the end-to-end leg: descriptors and initial state
+        uploaded every time)."""
+        if self.obj is not None:
+            self.obj.close()
+            self.obj = None
         if self.batch:
             self.obj = self.shll.Batch(self.items)
         else:
@@ -376,7 +396,7 @@ def main():
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        prob.reset()
+        prob.reset_from_host()
         prob.run()
         out = prob.result()
         torch.cuda.synchronize()
@@ -397,7 +417,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64"
             else args.precision, "data": "synthetic",
             "config": dict(config, cell_updates_per_run=prob.cu, precision=args.precision,
-                           fold_steps=args.fold or 16, parallelism=f"replicas{world}",
+                           fold_steps=args.fold or (64 if prob.dim == 1 else 16), parallelism=f"replicas{world}",
                            l2="flushed between runs (256 MB write)"),
             "roofline": roofline,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,

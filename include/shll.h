@@ -178,6 +178,11 @@ int shll_batch_item_status(shll_batch* b, int item);
 long shll_batch_cell_updates(const shll_batch* b);
 const char* shll_batch_last_error(const shll_batch* b);
 void shll_batch_destroy(shll_batch* b);
+/* Device-side checkpoint and restore of a mixed-precision 1D batch (no counterpart in the
+ * reference); restore also clears the breakdown flags raised after the checkpoint.
+ * SHLL_ERR_UNSUPPORTED for FP64 and 2D batches. */
+int shll_batch_checkpoint(shll_batch* b);
+int shll_batch_restore(shll_batch* b);
 
 /* ---- advancing a tube without allocating device memory ----
  * No counterpart in the reference (which has no GPU path).  For callers that cannot call
@@ -195,6 +200,12 @@ void shll_batch_destroy(shll_batch* b);
  * GPU (other threads, other streams) race with each other; serialise them.  Returns after the
  * work has completed. */
 int shll_tube_run_static(const shll_params* p, double* d_cons, long nsteps, void* stream);
+
+/* Replay of captured launch sequences (no counterpart in the reference): a mixed-precision 1D run
+ * is captured into a CUDA graph the first time its step counts and buffer parities occur and the
+ * graph is replayed by later identical runs.  on = 0 launches every run directly (default 1;
+ * process-wide). */
+void shll_set_graph_replay(int on);
 
 /* ---- the reference's own entry points on a process-wide default context ----
  * shll_ref_configure() chooses the problem (else base_shll.c's defaults, N = 256, F64). */

@@ -67,15 +67,32 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    inc = ["-I", os.path.join(HERE, "..", "include")]
+    link = ["-L", BUILD, f"-Wl,-rpath,{BUILD}"]
     # the reference-style C driver (host code in C over the C-ABI)
     drv = os.path.join(BUILD, "shll_tube")
     src = os.path.join(HERE, "host", "shll_tube.c")
     if _stale(drv, [src, LIB]):
-        cmd = ["gcc", "-O2", "-Wall", "-I", os.path.join(HERE, "..", "include"), src, "-o", drv,
-               "-L", BUILD, "-lshll_gb300", f"-Wl,-rpath,{BUILD}"]
+        cmd = ["gcc", "-O2", "-Wall"] + inc + [src, "-o", drv] + link + ["-lshll_gb300"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    # team-aware stages (OpenMP, base-omp's calling pattern) and their driver; skipped with a
+    # message where the C compiler has no OpenMP
+    omp_lib = os.path.join(BUILD, "libshll_gb300_omp.so")
+    omp_drv = os.path.join(BUILD, "shll_omp")
+    omp_src = os.path.join(HERE, "host", "shll_omp_stages.c")
+    drv_src = os.path.join(HERE, "host", "shll_omp.c")
+    if _stale(omp_lib, [omp_src, LIB]) or _stale(omp_drv, [drv_src, omp_src, LIB]):
+        cmds = [["gcc", "-O2", "-Wall", "-fopenmp", "-shared", "-fPIC"] + inc + [omp_src, "-o", omp_lib] + link
+                + ["-lshll_gb300"],
+                ["gcc", "-O2", "-Wall", "-fopenmp"] + inc + [drv_src, "-o", omp_drv] + link
+                + ["-lshll_gb300_omp", "-lshll_gb300"]]
+        for cmd in cmds:
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                print(f"OpenMP driver not built (gcc -fopenmp failed):\n{r.stderr}", file=sys.stderr)
+                break
     return LIB
 
 

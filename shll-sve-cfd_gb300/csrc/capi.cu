@@ -343,7 +343,9 @@ static int check_flag(shll_ctx* c) {
 }
 
 // uploads double primitive planes, then U from P and P from U (base_shll.c:202-205)
-static int load_primitives(shll_ctx* c, const double* prim) {
+// derive = false (plain paths only) leaves U to the caller's Compute_U_from_P, as the reference's
+// Allocate_and_Init_Memory does
+static int load_primitives(shll_ctx* c, const double* prim, bool derive = true) {
     const size_t n = (size_t)c->n, nv = c->nv;
     c->steps_taken = 0;
     c->fluxes_valid = false;
@@ -363,9 +365,11 @@ static int load_primitives(shll_ctx* c, const double* prim) {
     }
     CUDA_TRY(c, cudaMemcpyAsync(c->P, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
     c->cur = 0;
-    PlainArgs a = plain_args(c);
-    CUDA_TRY(c, plain_stage(c, a, STAGE_U_FROM_P));
-    CUDA_TRY(c, plain_stage(c, a, STAGE_P_FROM_U));
+    if (derive) {
+        PlainArgs a = plain_args(c);
+        CUDA_TRY(c, plain_stage(c, a, STAGE_U_FROM_P));
+        CUDA_TRY(c, plain_stage(c, a, STAGE_P_FROM_U));
+    }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->initialized = true;
     return check_flag(c);
@@ -621,10 +625,17 @@ extern "C" void Allocate_and_Init_Memory(void) {
     if (g_ref) { shll_destroy(g_ref); g_ref = nullptr; }
     int rc = shll_create(&g_ref_params, &g_ref);
     if (rc != SHLL_OK) { ref_fail("Allocate_and_Init_Memory", rc); return; }
-    // The reference only sets P here (its main then calls Compute_U_from_P and
-    // Compute_P_from_U); loading the primitives performs exactly those two stages, which the
-    // caller's own calls then repeat with identical results.
-    rc = shll_init_state(g_ref);
+    // The reference only sets P here; its main then calls Compute_U_from_P and Compute_P_from_U
+    // (base_shll.c:202-205).  The plain paths load P alone so that those calls are the first and
+    // only ones (in FP32 the U -> P -> U round trip is not idempotent); the mixed engine, which
+    // has no separate stages, initialises its state completely.
+    if (g_ref_params.ic.kind == SHLL_IC_USER) {
+        ref_fail("Allocate_and_Init_Memory", SHLL_ERR_STATE);
+        return;
+    }
+    std::vector<double> prim((size_t)g_ref->nv * g_ref->n);
+    shll_ic_fill(&g_ref->p, g_ref->real_bits, prim.data());
+    rc = load_primitives(g_ref, prim.data(), !g_ref->plain);
     if (rc != SHLL_OK) ref_fail("Allocate_and_Init_Memory", rc);
 }
 #define REF_STAGE(NAME, CALL)                                      \
@@ -745,6 +756,21 @@ extern "C" long shll_batch_cell_updates(const shll_batch* b) {
     return b->pb ? plain_batch_cell_updates(b->pb) : mixed_cell_updates(b->m);
 }
 extern "C" const char* shll_batch_last_error(const shll_batch* b) { return b ? b->err : "no batch"; }
+
+// device-side checkpoint / restore of a mixed-precision 1D batch (restore also clears the
+// breakdown flags raised after the checkpoint)
+extern "C" int shll_batch_checkpoint(shll_batch* b) {
+    if (!b) return SHLL_ERR_ARG;
+    if (!b->m) { snprintf(b->err, sizeof(b->err), "checkpoint needs a mixed-precision batch"); return SHLL_ERR_UNSUPPORTED; }
+    if (!b->loaded) { snprintf(b->err, sizeof(b->err), "batch not loaded"); return SHLL_ERR_STATE; }
+    return mixed_checkpoint(b->m, false, b->err, sizeof(b->err));
+}
+
+extern "C" int shll_batch_restore(shll_batch* b) {
+    if (!b) return SHLL_ERR_ARG;
+    if (!b->m) { snprintf(b->err, sizeof(b->err), "restore needs a mixed-precision batch"); return SHLL_ERR_UNSUPPORTED; }
+    return mixed_checkpoint(b->m, true, b->err, sizeof(b->err));
+}
 
 extern "C" void shll_batch_destroy(shll_batch* b) {
     if (!b) return;

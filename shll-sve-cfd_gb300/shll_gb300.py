@@ -55,7 +55,8 @@ EXPORTS = [
     "shll_batch_destroy", "shll_ref_configure", "shll_ref_context", "Allocate_and_Init_Memory",
     "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P", "Update_U_from_F", "Save_Results",
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
-    "shll_batch_set_stream", "shll_batch_item_status",
+    "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
+    "shll_batch_restore",
 ]
 
 
@@ -144,6 +145,11 @@ def steps_for(p):
 
 def kernel_launches():
     return lib().shll_kernel_launches()
+
+
+def set_graph_replay(on):
+    """Replay captured launch sequences of repeated mixed-precision 1D runs (default on)."""
+    lib().shll_set_graph_replay(1 if on else 0)
 
 
 class Context:
@@ -272,6 +278,14 @@ class Batch:
             return rc
         self._ck(rc, "batch_run")
         return rc
+
+    def checkpoint(self):
+        """Device-side copy of the state (mixed-precision 1D batches)."""
+        return self._ck(lib().shll_batch_checkpoint(self.h), "batch_checkpoint")
+
+    def restore(self):
+        """Back to the last checkpoint (also clears breakdown flags raised since)."""
+        return self._ck(lib().shll_batch_restore(self.h), "batch_restore")
 
     def item_status(self, i):
         return lib().shll_batch_item_status(self.h, i)

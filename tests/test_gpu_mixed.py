@@ -105,3 +105,18 @@ def test_single_tube_breakdown_is_reported(shll, oracle, prec):
     with pytest.raises(shll.ShllError) as e:
         c.run()
     assert e.value.status == shll.ERR_NUMERIC
+
+
+def test_repeated_run_replays_identically(shll):
+    # The first run's launch sequence is captured into a CUDA graph; a run with the same step
+    # counts and buffer parity replays it and must give the same bits.
+    c = shll.Context(shll.params(1, 2, nx=3000, precision="mixed_f64"))
+    c.init_state()
+    c.checkpoint()
+    c.run()
+    first = c.primitives()
+    n1 = shll.kernel_launches()
+    c.restore()
+    c.run()
+    assert np.array_equal(c.primitives(), first)
+    assert shll.kernel_launches() - n1 > 100   # the replay counts its launches too
