@@ -72,6 +72,18 @@ struct Frame2 {
     AnchorCoef cx, cy;               // coefficients for the x and y split fluxes
 };
 
+// What a step needs of its tile's frame, as FP32 values and pairs (written once per fold window by
+// k_tileconst2d, so that no step does FP64 arithmetic)
+struct TileC2 {
+    AnchorCoef cx, cy;      // split-flux coefficients (x, y)
+    float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
+    float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
+    float dn[4][4][2];      // U*(neighbour) - U*(this) as pairs: [west, east, south, north][comp]
+};
+constexpr int kTileC2Words = (int)(sizeof(TileC2) / 4);
+constexpr int kTileC2ConstOff = (int)(2 * sizeof(AnchorCoef) / 4);  // first word of wc
+static_assert(sizeof(TileC2) % 4 == 0, "word copy");
+
 __device__ void make_frame2(Frame2& f, const double U[4], const Dom2& d) {
     const double rho = U[0], m = U[1], nn = U[2], E = U[3];
     const double u = m / rho, v = nn / rho, e = E / rho;
@@ -177,6 +189,7 @@ struct Args2 {
     const Dom2* doms;
     const TileD* tiles;
     Frame2* frames;      // per tile, written by the fold
+    TileC2* tc;          // per tile, derived from the frames after each fold
     void* B;             // stored state: double[4][plane] or FP32 value planes (KAHAN)
     float* Blo;          // FP32 compensation planes (KAHAN)
     float* C;            // float[4][plane]: B - U*(tile) at the last fold
@@ -223,10 +236,11 @@ __device__ __forceinline__ void edge_correction(const Args2& A, const Dom2& D, i
 
 __device__ __forceinline__ bool on_edge_line(int i, int j) { return (i > 0 && i % TI == 0) || (j > 0 && j % TJ == 0); }
 
-// (th, tl) = lam * x as an FP32 pair (exact when lam is an FP32 power of two)
+// (th, tl) = lam * x as an FP32 pair (exact, tl = 0, when lam is an FP32 power of two: POW2)
+template <bool POW2 = false>
 __device__ __forceinline__ void lam_mul(float lh, float ll, float x, float& th, float& tl) {
     th = __fmul_rn(lh, x);
-    tl = __fadd_rn(__fmaf_rn(lh, x, -th), __fmul_rn(ll, x));
+    tl = POW2 ? 0.f : __fadd_rn(__fmaf_rn(lh, x, -th), __fmul_rn(ll, x));
 }
 
 // ---- fold: B += P (+ the last edge corrections), new frames, C = B - U* ----
@@ -295,8 +309,42 @@ __global__ void __launch_bounds__(NT) k_fold2d(Args2 A) {
     }
 }
 
+// ---- per-tile step constants of the new frames (after a fold) ----
+__global__ void __launch_bounds__(32) k_tileconst2d(Args2 A) {
+    const TileD tile = A.tiles[blockIdx.x];
+    const Dom2 D = A.doms[tile.dom];
+    const int wd = min(max(D.steps - A.s0, 0), A.win);
+    if (A.win > 0 && wd == 0) return;   // frame unchanged
+    const int tid = threadIdx.x;
+    const int tb = D.tile_base + tile.ti * D.tiles_j + tile.tj;
+    const Frame2& f = A.frames[tb];
+    TileC2& c = A.tc[tb];
+    for (int q = tid; q < kTileC2ConstOff; q += 32)
+        reinterpret_cast<float*>(&c)[q] = q < (int)(sizeof(AnchorCoef) / 4)
+            ? reinterpret_cast<const float*>(&f.cx)[q] : reinterpret_cast<const float*>(&f.cy)[q - sizeof(AnchorCoef) / 4];
+    if (tid < 16) {
+        // constant wall terms: lam*(W_const - Fref) (west/south), lam*(Fref - W_const) (east/north)
+        const int w = tid / 4, k = tid % 4;
+        double v;
+        if (w == 0) v = k == 1 ? D.lamx * (2.0 * f.fmS1 - f.Fx[1]) : -D.lamx * f.Fx[k];
+        else if (w == 1) v = k == 1 ? D.lamx * (f.Fx[1] - 2.0 * f.fpS1) : D.lamx * f.Fx[k];
+        else if (w == 2) v = k == 2 ? D.lamy * (2.0 * f.hmS2 - f.Fy[2]) : -D.lamy * f.Fy[k];
+        else v = k == 2 ? D.lamy * (f.Fy[2] - 2.0 * f.hpS2) : D.lamy * f.Fy[k];
+        split2(v, c.wc[w][k][0], c.wc[w][k][1]);
+        if (tid < 8) {
+            const int dir = tid / 4;
+            split2(dir == 0 ? D.lamx * f.Fx[k] : D.lamy * f.Fy[k], c.lf[dir][k][0], c.lf[dir][k][1]);
+        }
+        // frame of the neighbour tile w (0 west = ti-1, 1 east, 2 south = tj-1, 3 north)
+        const int ti = tile.ti + (w == 0 ? -1 : w == 1 ? 1 : 0), tj = tile.tj + (w == 2 ? -1 : w == 3 ? 1 : 0);
+        double dU = 0.0;
+        if (ti >= 0 && ti < D.tiles_i && tj >= 0 && tj < D.tiles_j)
+            dU = A.frames[D.tile_base + ti * D.tiles_j + tj].U[k] - f.U[k];
+        split2(dU, c.dn[w][k][0], c.dn[w][k][1]);
+    }
+}
+
 struct Smem2 {
-    Frame2 fr;
     float f[16][WI * WJ];   // dfp0..3, dfm0..3, dhp0..3, dhm0..3 of the window (tile + 1-cell halo)
     float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
     float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
@@ -304,7 +352,7 @@ struct Smem2 {
 };
 
 // ---- one time step of one tile ----
-template <bool KAHAN>
+template <bool KAHAN, bool LAM_POW2>
 __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
     __shared__ Smem2 S;
     const TileD tile = A.tiles[blockIdx.x];
@@ -322,34 +370,11 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
     float* plo = (kw & 1) ? A.Pl[0] : A.Pl[1];
     const int pp = (A.step - 1) & 1;                     // edge buffers of the previous step
     const float lxh = D.lxh, lxl = D.lxl, lyh = D.lyh, lyl = D.lyl;
-
-    // frame of this tile (written by the last fold)
-    static_assert(sizeof(Frame2) % 8 == 0, "frame copied as doubles");
-    for (int q = tid; q < (int)(sizeof(Frame2) / 8); q += NT)
-        reinterpret_cast<double*>(&S.fr)[q] = reinterpret_cast<const double*>(&A.frames[tb])[q];
-    __syncthreads();
-    if (tid < 16) {
-        // constant wall terms: lam*(W_const - Fref) (west/south), lam*(Fref - W_const) (east/north)
-        const int w = tid / 4, k = tid % 4;
-        const Frame2& f = S.fr;
-        double v;
-        if (w == 0) v = k == 1 ? D.lamx * (2.0 * f.fmS1 - f.Fx[1]) : -D.lamx * f.Fx[k];
-        else if (w == 1) v = k == 1 ? D.lamx * (f.Fx[1] - 2.0 * f.fpS1) : D.lamx * f.Fx[k];
-        else if (w == 2) v = k == 2 ? D.lamy * (2.0 * f.hmS2 - f.Fy[2]) : -D.lamy * f.Fy[k];
-        else v = k == 2 ? D.lamy * (f.Fy[2] - 2.0 * f.hpS2) : D.lamy * f.Fy[k];
-        split2(v, S.wc[w][k][0], S.wc[w][k][1]);
-        if (tid < 8) {
-            const int dir = tid / 4;
-            split2(dir == 0 ? D.lamx * f.Fx[k] : D.lamy * f.Fy[k], S.lf[dir][k][0], S.lf[dir][k][1]);
-        }
-        // frame of the neighbour tile w (0 west = ti-1, 1 east, 2 south = tj-1, 3 north)
-        const int ti = tile.ti + (w == 0 ? -1 : w == 1 ? 1 : 0), tj = tile.tj + (w == 2 ? -1 : w == 3 ? 1 : 0);
-        double dU = 0.0;
-        if (ti >= 0 && ti < D.tiles_i && tj >= 0 && tj < D.tiles_j)
-            dU = A.frames[D.tile_base + ti * D.tiles_j + tj].U[k] - f.U[k];
-        split2(dU, S.dn[w][k][0], S.dn[w][k][1]);
-    }
-    __syncthreads();
+    // the tile's step constants (one word per thread; read after the barrier below), and its
+    // split-flux coefficients straight from the table (the same words for every thread)
+    const TileC2& tc = A.tc[tb];
+    if (tid < kTileC2Words - kTileC2ConstOff)
+        reinterpret_cast<float*>(&S.wc)[tid] = reinterpret_cast<const float*>(&tc)[kTileC2ConstOff + tid];
     const int li = tid / TJ, lj = tid % TJ;
     const int i = i0 + li, j = j0 + lj;
     const bool own = li < hi_i && lj < hi_j;
@@ -387,10 +412,10 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
                 // deviation from this tile's frame: C (relative to the owner's frame) + the owner's
                 // frame offset + the increments
                 float base = A.C[idx];
-                if (nb >= 0) base = __fadd_rn(__fadd_rn(base, S.dn[nb][k][0]), S.dn[nb][k][1]);
+                if (nb >= 0) base = __fadd_rn(__fadd_rn(base, tc.dn[nb][k][0]), tc.dn[nb][k][1]);
                 d[k] = __fadd_rn(base, __fadd_rn(h, l));
             }
-            dflux2(S.fr.cx, S.fr.cy, d, dfp, dfm, dhp, dhm);
+            dflux2(tc.cx, tc.cy, d, dfp, dfm, dhp, dhm);
         }
         if (wi >= 0) {
             const int w = wi * WJ + wj;
@@ -415,42 +440,42 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
         // x west
         if (i > 0) {
             const float Dw = __fadd_rn(S.f[k][wW], fm);
-            lam_mul(lxh, lxl, Dw, th, tl);
-            two_sum_acc(ah, al, th); al = __fadd_rn(al, tl);
+            lam_mul<LAM_POW2>(lxh, lxl, Dw, th, tl);
+            two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl);
             if (li == 0) { float* r = exo[D.ex_base + (i / TI - 1) * D.ny + j].r[1][k]; ff_add(S.lf[0][k][0], S.lf[0][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[0][k][0]); al = __fadd_rn(al, S.wc[0][k][1]);
-            if (k == 1) { lam_mul(lxh, lxl, __fmul_rn(2.f, fm), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
+            if (k == 1) { lam_mul<LAM_POW2>(lxh, lxl, __fmul_rn(2.f, fm), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
         }
         // x east
         if (i < D.nx - 1) {
             const float De = __fadd_rn(fp, S.f[4 + k][wE]);
-            lam_mul(lxh, lxl, De, th, tl);
-            two_sum_acc(ah, al, -th); al = __fadd_rn(al, -tl);
+            lam_mul<LAM_POW2>(lxh, lxl, De, th, tl);
+            two_sum_acc(ah, al, -th); if (!LAM_POW2) al = __fadd_rn(al, -tl);
             if (li == hi_i - 1) { float* r = exo[D.ex_base + ((i + 1) / TI - 1) * D.ny + j].r[0][k]; ff_add(S.lf[0][k][0], S.lf[0][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[1][k][0]); al = __fadd_rn(al, S.wc[1][k][1]);
-            if (k == 1) { lam_mul(lxh, lxl, -__fmul_rn(2.f, fp), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
+            if (k == 1) { lam_mul<LAM_POW2>(lxh, lxl, -__fmul_rn(2.f, fp), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
         }
         // y south
         if (j > 0) {
             const float Ds = __fadd_rn(S.f[8 + k][wS], hm);
-            lam_mul(lyh, lyl, Ds, th, tl);
-            two_sum_acc(ah, al, th); al = __fadd_rn(al, tl);
+            lam_mul<LAM_POW2>(lyh, lyl, Ds, th, tl);
+            two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl);
             if (lj == 0) { float* r = eyo[D.ey_base + (j / TJ - 1) * D.nx + i].r[1][k]; ff_add(S.lf[1][k][0], S.lf[1][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[2][k][0]); al = __fadd_rn(al, S.wc[2][k][1]);
-            if (k == 2) { lam_mul(lyh, lyl, __fmul_rn(2.f, hm), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
+            if (k == 2) { lam_mul<LAM_POW2>(lyh, lyl, __fmul_rn(2.f, hm), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
         }
         // y north
         if (j < D.ny - 1) {
             const float Dn = __fadd_rn(hp, S.f[12 + k][wN]);
-            lam_mul(lyh, lyl, Dn, th, tl);
-            two_sum_acc(ah, al, -th); al = __fadd_rn(al, -tl);
+            lam_mul<LAM_POW2>(lyh, lyl, Dn, th, tl);
+            two_sum_acc(ah, al, -th); if (!LAM_POW2) al = __fadd_rn(al, -tl);
             if (lj == hi_j - 1) { float* r = eyo[D.ey_base + ((j + 1) / TJ - 1) * D.nx + i].r[0][k]; ff_add(S.lf[1][k][0], S.lf[1][k][1], th, tl, r[0], r[1]); }
         } else {
             two_sum_acc(ah, al, S.wc[3][k][0]); al = __fadd_rn(al, S.wc[3][k][1]);
-            if (k == 2) { lam_mul(lyh, lyl, -__fmul_rn(2.f, hp), th, tl); two_sum_acc(ah, al, th); al = __fadd_rn(al, tl); }
+            if (k == 2) { lam_mul<LAM_POW2>(lyh, lyl, -__fmul_rn(2.f, hp), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
         }
         pho[k * P + cell] = ah;
         plo[k * P + cell] = al;
@@ -472,6 +497,7 @@ struct Mixed2D {
     Edge* ex[2] = {nullptr, nullptr};
     Edge* ey[2] = {nullptr, nullptr};
     Frame2* frames = nullptr;
+    TileC2* tc = nullptr;
     Dom2* d_doms = nullptr;
     TileD* d_tiles = nullptr;
     int fold = 16;
@@ -543,6 +569,7 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
         if (ok) ok = cudaMalloc(&d->ey[b], sizeof(Edge) * d->ney) == cudaSuccess;
     }
     if (ok) ok = cudaMalloc(&d->frames, sizeof(Frame2) * d->tiles.size()) == cudaSuccess;
+    if (ok) ok = cudaMalloc(&d->tc, sizeof(TileC2) * d->tiles.size()) == cudaSuccess;
     if (ok) ok = cudaMalloc(&d->d_doms, sizeof(Dom2) * count) == cudaSuccess;
     if (ok) ok = cudaMalloc(&d->d_tiles, sizeof(TileD) * d->tiles.size()) == cudaSuccess;
     if (ok) ok = cudaMemcpy(d->d_tiles, d->tiles.data(), sizeof(TileD) * d->tiles.size(), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -560,6 +587,7 @@ void mixed2d_detach(MixedState* m) {
     cudaFree(d->B); cudaFree(d->Blo); cudaFree(d->C);
     for (int b = 0; b < 2; b++) { cudaFree(d->Ph[b]); cudaFree(d->Pl[b]); cudaFree(d->ex[b]); cudaFree(d->ey[b]); }
     cudaFree(d->frames);
+    cudaFree(d->tc);
     cudaFree(d->d_doms);
     cudaFree(d->d_tiles);
     delete d;
@@ -624,6 +652,7 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
     A.doms = d->d_doms;
     A.tiles = d->d_tiles;
     A.frames = d->frames;
+    A.tc = d->tc;
     A.B = d->B; A.Blo = d->Blo; A.C = d->C;
     A.Ph[0] = d->Ph[0]; A.Ph[1] = d->Ph[1];
     A.Pl[0] = d->Pl[0]; A.Pl[1] = d->Pl[1];
@@ -640,15 +669,27 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
         A.win = win;
         if (kahan) k_fold2d<true><<<ntiles, NT, 0, s>>>(A);
         else k_fold2d<false><<<ntiles, NT, 0, s>>>(A);
-        launches++;
+        k_tileconst2d<<<ntiles, 32, 0, s>>>(A);
+        launches += 2;
     };
+    // lam_x and lam_y powers of two for every domain: the interface terms lam*Delta are exact
+    bool pow2 = true;
+    for (const Dom2& D : d->doms) {
+        int ex;
+        pow2 = pow2 && std::frexp(D.lamx, &ex) == 0.5 && std::frexp(D.lamy, &ex) == 0.5;
+    }
     fold(0, 0);  // frames and C of the current state
     int s0 = 0;
     for (long st = 0; st < maxsteps; st++) {
         A.step = (int)st;
         A.s0 = s0;
-        if (kahan) k_step2d<true><<<ntiles, NT, 0, s>>>(A);
-        else k_step2d<false><<<ntiles, NT, 0, s>>>(A);
+        if (kahan) {
+            if (pow2) k_step2d<true, true><<<ntiles, NT, 0, s>>>(A);
+            else k_step2d<true, false><<<ntiles, NT, 0, s>>>(A);
+        } else {
+            if (pow2) k_step2d<false, true><<<ntiles, NT, 0, s>>>(A);
+            else k_step2d<false, false><<<ntiles, NT, 0, s>>>(A);
+        }
         launches++;
         if (st + 1 - s0 == d->fold || st + 1 == maxsteps) {
             fold(s0, (int)(st + 1 - s0));
