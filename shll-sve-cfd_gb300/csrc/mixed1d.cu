@@ -167,9 +167,6 @@ struct Smem1 {
 constexpr int kFrameWords = (int)(sizeof(Frame1) / 4);
 static_assert(sizeof(Frame1) % 4 == 0 && kFrameWords <= MT, "frame copy by one word per thread");
 
-// lane q of a float2
-__device__ __forceinline__ float lane(float2 v, int q) { return q ? v.y : v.x; }
-__device__ __forceinline__ void set_lane(float2& v, int q, float x) { if (q) v.y = x; else v.x = x; }
 
 // One sweep of one chunk.  Thread t holds window cells w0 = 2t and w0 + 1 as the two lanes of
 // FP32x2 registers.  Per step: split-flux deviations of both cells (packed) -> shared memory

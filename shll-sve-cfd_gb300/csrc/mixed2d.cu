@@ -183,6 +183,82 @@ __device__ __forceinline__ void dflux2(const AnchorCoef& cx, const AnchorCoef& c
 }
 
 
+// anchor coefficients of a 2D tile frame, each duplicated into both FP32x2 lanes
+struct Coef2D {
+    float2 rho, u, v, nu, nv, ne, T, a, gR, R, cvinv, P, m, n, E;
+    float2 Mx, nMx, Z1x, Z2x, My, nMy, Z1y, Z2y;
+    float2 Fx[4], Fy[4], Uf[4];
+};
+__device__ __forceinline__ Coef2D coef2d(const AnchorCoef& cx, const AnchorCoef& cy) {
+    Coef2D k;
+    k.rho = f2(cx.rho); k.u = f2(cx.u); k.v = f2(cx.v); k.nu = f2(-cx.u); k.nv = f2(-cx.v); k.ne = f2(-cx.e);
+    k.T = f2(cx.T); k.a = f2(cx.a); k.gR = f2(cx.gR); k.R = f2(cx.R); k.cvinv = f2(cx.cvinv); k.P = f2(cx.P);
+    k.m = f2(cx.Uf[1]); k.n = f2(cx.Uf[2]); k.E = f2(cx.Uf[3]);
+    k.Mx = f2(cx.M); k.nMx = f2(-cx.M); k.Z1x = f2(cx.Z1); k.Z2x = f2(cx.Z2);
+    k.My = f2(cy.M); k.nMy = f2(-cy.M); k.Z1y = f2(cy.Z1); k.Z2y = f2(cy.Z2);
+    for (int q = 0; q < 4; q++) { k.Fx[q] = f2(cx.F[q]); k.Fy[q] = f2(cy.F[q]); k.Uf[q] = f2(cx.Uf[q]); }
+    return k;
+}
+
+// dflux2 for two cells at once (same deviation identities, lane by lane; the minus fluxes from
+// dfp + dfm = dF)
+__device__ __forceinline__ void dflux2x2(const Coef2D& c, const float2 d[4], float2 fp[4], float2 fm[4],
+                                         float2 hp[4], float2 hm[4]) {
+    const float2 drho = d[0], dm = d[1], dn = d[2], dE = d[3];
+    const float2 rho = add2(c.rho, drho);
+    const float2 r = rcp2(rho);
+    const float2 du = mul2(fma2(c.nu, drho, dm), r);
+    const float2 dv = mul2(fma2(c.nv, drho, dn), r);
+    const float2 u = add2(c.u, du), v = add2(c.v, dv);
+    const float2 de = mul2(fma2(c.ne, drho, dE), r);
+    const float2 ke = fma2(add2(u, c.u), du, mul2(add2(v, c.v), dv));  // d(u^2 + v^2)
+    const float2 dT = mul2(fma2(f2(-0.5f), ke, de), c.cvinv);
+    const float2 T = add2(c.T, dT);
+    const float2 gRT = mul2(c.gR, T);
+    const float2 ainv = rsqrt2(gRT);
+    const float2 a = mul2(gRT, ainv);
+    const float2 da = mul2(mul2(c.gR, dT), rcp2(add2(a, c.a)));
+    const float2 dP = mul2(c.R, fma2(drho, T, mul2(c.rho, dT)));
+    const float2 P = add2(c.P, dP);
+    const float2 EP = add2(add2(c.E, dE), P), dEP = add2(dE, dP);
+    {   // x direction, M = u / a
+        const float2 dM = mul2(fma2(c.nMx, da, du), ainv);
+        const float2 M = add2(c.Mx, dM);
+        const float2 dZ1 = mul2(f2(0.5f), dM);
+        const float2 Z1 = add2(c.Z1x, dZ1);
+        const float2 dZ2 = mul2(f2(0.5f), fma2(da, fma2(neg2(M), M, f2(1.0f)), neg2(mul2(mul2(c.a, add2(M, c.Mx)), dM))));
+        const float2 Z2 = add2(c.Z2x, dZ2);
+        float2 dF[4];
+        dF[0] = dm;
+        dF[1] = add2(fma2(dm, u, mul2(c.m, du)), dP);
+        dF[2] = fma2(dm, v, mul2(c.m, dv));
+        dF[3] = fma2(du, EP, mul2(c.u, dEP));
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            fp[k] = add2(fma2(dF[k], Z1, mul2(c.Fx[k], dZ1)), fma2(d[k], Z2, mul2(c.Uf[k], dZ2)));
+            fm[k] = sub2(dF[k], fp[k]);
+        }
+    }
+    {   // y direction, M = v / a
+        const float2 dM = mul2(fma2(c.nMy, da, dv), ainv);
+        const float2 M = add2(c.My, dM);
+        const float2 dZ1 = mul2(f2(0.5f), dM);
+        const float2 Z1 = add2(c.Z1y, dZ1);
+        const float2 dZ2 = mul2(f2(0.5f), fma2(da, fma2(neg2(M), M, f2(1.0f)), neg2(mul2(mul2(c.a, add2(M, c.My)), dM))));
+        const float2 Z2 = add2(c.Z2y, dZ2);
+        float2 dH[4];
+        dH[0] = dn;
+        dH[1] = fma2(dn, u, mul2(c.n, du));
+        dH[2] = add2(fma2(dn, v, mul2(c.n, dv)), dP);
+        dH[3] = fma2(dv, EP, mul2(c.v, dEP));
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            hp[k] = add2(fma2(dH[k], Z1, mul2(c.Fy[k], dZ1)), fma2(d[k], Z2, mul2(c.Uf[k], dZ2)));
+            hm[k] = sub2(dH[k], hp[k]);
+        }
+    }
+}
+
 // Cell and plane offsets fit in 32 bits (the host refuses batches of more than 2^29 cells), so
 // the kernels index with int: 64-bit integer multiply-adds would run on the slow FP64 pipe.
 struct Args2 {
@@ -344,16 +420,24 @@ __global__ void __launch_bounds__(32) k_tileconst2d(Args2 A) {
     }
 }
 
+// ---- one time step of one tile (packed: two cells per thread along j) ----
+// 320 threads: threads 0..255 own the tile's 16 x 16 cell pairs (cells j, j+1 of a row); threads
+// 256..319 evaluate the 64 halo pairs (the rows west and east of the tile, the column pairs south
+// (j0-2, j0-1) and north (j0+32, j0+33)).  Every thread evaluates one pair's split fluxes, then,
+// after the one barrier, each owner thread sums its pair's four interfaces per component.
+constexpr int NTP = 320;
+constexpr int WR = TI + 2;        // window rows (i0-1 .. i0+TI)
+constexpr int WP = TJ / 2 + 2;    // window pairs per row (cells j0-2 .. j0+TJ+1)
+
 struct Smem2 {
-    float f[16][WI * WJ];   // dfp0..3, dfm0..3, dhp0..3, dhm0..3 of the window (tile + 1-cell halo)
+    float2 f[16][WR][WP];   // dfp0..3, dfm0..3, dhp0..3, dhm0..3 of the window pairs
     float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
     float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
     float dn[4][4][2];      // U*(neighbour) - U*(this) as pairs: [west, east, south, north][comp]
 };
 
-// ---- one time step of one tile ----
 template <bool KAHAN, bool LAM_POW2>
-__global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
+__global__ void __launch_bounds__(NTP) k_step2d(Args2 A) {
     __shared__ Smem2 S;
     const TileD tile = A.tiles[blockIdx.x];
     const Dom2 D = A.doms[tile.dom];
@@ -369,116 +453,170 @@ __global__ void __launch_bounds__(NT) k_step2d(Args2 A) {
     float* pho = (kw & 1) ? A.Ph[0] : A.Ph[1];
     float* plo = (kw & 1) ? A.Pl[0] : A.Pl[1];
     const int pp = (A.step - 1) & 1;                     // edge buffers of the previous step
-    const float lxh = D.lxh, lxl = D.lxl, lyh = D.lyh, lyl = D.lyl;
     // the tile's step constants (one word per thread; read after the barrier below), and its
-    // split-flux coefficients straight from the table (the same words for every thread)
+    // split-flux coefficients from the table (the same words for every thread)
     const TileC2& tc = A.tc[tb];
     if (tid < kTileC2Words - kTileC2ConstOff)
         reinterpret_cast<float*>(&S.wc)[tid] = reinterpret_cast<const float*>(&tc)[kTileC2ConstOff + tid];
-    const int li = tid / TJ, lj = tid % TJ;
-    const int i = i0 + li, j = j0 + lj;
-    const bool own = li < hi_i && lj < hi_j;
-    float Ph[4] = {0, 0, 0, 0}, Pl[4] = {0, 0, 0, 0};   // own increment pair
-    for (int slot = 0; slot < 2; slot++) {
-        int wi, wj;   // window coordinates
-        bool act;
-        if (slot == 0) {
-            wi = li + 1; wj = lj + 1; act = own;
-        } else {
-            const int h = tid;
-            // halo rows above/below the tile (columns 1..hi_j) and columns left/right (rows 1..hi_i)
-            if (h < TJ) { wi = 0; wj = h + 1; act = h < hi_j && i0 > 0; }
-            else if (h < 2 * TJ) { wi = hi_i + 1; wj = h - TJ + 1; act = h - TJ < hi_j && i0 + hi_i < D.nx; }
-            else if (h < 2 * TJ + TI) { wi = h - 2 * TJ + 1; wj = 0; act = h - 2 * TJ < hi_i && j0 > 0; }
-            else if (h < 2 * TJ + 2 * TI) { wi = h - 2 * TJ - TI + 1; wj = hi_j + 1; act = h - 2 * TJ - TI < hi_i && j0 + hi_j < D.ny; }
-            else { wi = -1; wj = -1; act = false; }
-        }
-        float dfp[4] = {0, 0, 0, 0}, dfm[4] = {0, 0, 0, 0}, dhp[4] = {0, 0, 0, 0}, dhm[4] = {0, 0, 0, 0};
+    const Coef2D c2 = coef2d(tc.cx, tc.cy);
+
+    // ---- this thread's window pair ----
+    int r, c, nb;   // window row and pair column; owner tile of the cells (-1 this, 0 W, 1 E, 2 S, 3 N)
+    bool act;
+    if (tid < 256) {
+        r = (tid >> 4) + 1; c = (tid & 15) + 1; nb = -1;
+        act = r - 1 < hi_i && 2 * (c - 1) < hi_j;
+    } else {
+        const int h = tid - 256;
+        if (h < 16) { r = 0; c = h + 1; nb = 0; act = i0 > 0 && 2 * h < hi_j; }
+        else if (h < 32) { r = hi_i + 1; c = h - 15; nb = 1; act = i0 + hi_i < D.nx && 2 * (h - 16) < hi_j; }
+        else if (h < 48) { r = h - 31; c = 0; nb = 2; act = j0 > 0 && h - 32 < hi_i; }
+        else { r = h - 47; c = WP - 1; nb = 3; act = j0 + hi_j < D.ny && h - 48 < hi_i; }
+    }
+    const int ci = i0 + r - 1, cj = j0 + 2 * c - 2;     // cell of lane x; lane y is (ci, cj + 1)
+    float2 Ph[4], Pl[4];                                 // own increment pairs
+    {
+        float2 fp[4], fm[4], hp[4], hm[4];
+        float2 d[4];
+        for (int k = 0; k < 4; k++) { d[k] = f2(0.f); Ph[k] = f2(0.f); Pl[k] = f2(0.f); }
         if (act) {
-            const int ci = i0 + wi - 1, cj = j0 + wj - 1;
-            const int cell = D.base + ci * D.ny + cj;
-            // tile that owns the cell: this one (slot 0) or the west/east/south/north neighbour
-            const int nb = slot == 0 ? -1 : (wi == 0 ? 0 : wi == hi_i + 1 ? 1 : wj == 0 ? 2 : 3);
-            float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
-            if (kw > 0 && on_edge_line(ci, cj)) edge_correction(A, D, ci, cj, pp, ch, cl);
-            float d[4];
-            for (int k = 0; k < 4; k++) {
-                const int idx = k * P + cell;
-                float h = 0.f, l = 0.f;
-                if (kw > 0) { h = phi[idx]; l = pli[idx]; }
-                two_sum_acc(h, l, ch[k]);   // the pending edge correction joins the increment pair
-                l = __fadd_rn(l, cl[k]);
-                if (slot == 0) { Ph[k] = h; Pl[k] = l; }
-                // deviation from this tile's frame: C (relative to the owner's frame) + the owner's
-                // frame offset + the increments
-                float base = A.C[idx];
-                if (nb >= 0) base = __fadd_rn(__fadd_rn(base, tc.dn[nb][k][0]), tc.dn[nb][k][1]);
-                d[k] = __fadd_rn(base, __fadd_rn(h, l));
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int cjq = cj + q;
+                if (cjq < 0 || cjq >= D.ny) continue;    // outside the domain: zero deviation
+                const int cell = D.base + ci * D.ny + cjq;
+                float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
+                if (kw > 0 && on_edge_line(ci, cjq)) edge_correction(A, D, ci, cjq, pp, ch, cl);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int idx = k * P + cell;
+                    float h = 0.f, l = 0.f;
+                    if (kw > 0) { h = phi[idx]; l = pli[idx]; }
+                    two_sum_acc(h, l, ch[k]);   // the pending edge correction joins the increment pair
+                    l = __fadd_rn(l, cl[k]);
+                    if (nb < 0) { set_lane(Ph[k], q, h); set_lane(Pl[k], q, l); }
+                    // deviation from this tile's frame: C (relative to the owner's frame) + the
+                    // owner's frame offset + the increments
+                    float base = A.C[idx];
+                    if (nb >= 0) base = __fadd_rn(__fadd_rn(base, tc.dn[nb][k][0]), tc.dn[nb][k][1]);
+                    set_lane(d[k], q, __fadd_rn(base, __fadd_rn(h, l)));
+                }
             }
-            dflux2(tc.cx, tc.cy, d, dfp, dfm, dhp, dhm);
         }
-        if (wi >= 0) {
-            const int w = wi * WJ + wj;
+        dflux2x2(c2, d, fp, fm, hp, hm);
+        // every slot is written (inactive pairs with the frame's own zero deviations, so that a
+        // masked-out neighbour read is finite), except that in a tile cut short in i the east halo
+        // row coincides with the first unowned row: there the halo thread writes
+        if (!(nb < 0 && r == hi_i + 1)) {
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                S.f[k][w] = dfp[k]; S.f[4 + k][w] = dfm[k]; S.f[8 + k][w] = dhp[k]; S.f[12 + k][w] = dhm[k];
+                S.f[k][r][c] = fp[k]; S.f[4 + k][r][c] = fm[k]; S.f[8 + k][r][c] = hp[k]; S.f[12 + k][r][c] = hm[k];
             }
         }
     }
     __syncthreads();
-    if (!own) return;
-    // ---- interface terms and the increment of the own cell ----
-    const int w = (li + 1) * WJ + (lj + 1);
-    const int wW = w - WJ, wE = w + WJ, wS = w - 1, wN = w + 1;
+    if (nb >= 0 || !act) return;
+
+    // ---- interface terms and the increments of the own pair ----
+    const int i = ci, jx = cj;                           // lane y: column jx + 1
+    const bool has_y = jx + 1 < j0 + hi_j;
+    const float2 lx2 = f2(D.lxh), lxl2 = f2(D.lxl), ly2 = f2(D.lyh), lyl2 = f2(D.lyl);
+    // y walls: lane x at j = 0 (south), the lane at j = ny - 1 (north); their regular south / north
+    // terms are masked and replaced by the wall terms below
+    const bool wS = jx == 0, wNx = jx == D.ny - 1, wNy = has_y && jx + 1 == D.ny - 1;
+    const float2 mS = make_float2(wS ? 0.f : 1.f, 1.f), mN = make_float2(wNx ? 0.f : 1.f, wNy ? 0.f : 1.f);
     Edge* exo = A.step & 1 ? A.ex[1] : A.ex[0];
     Edge* eyo = A.step & 1 ? A.ey[1] : A.ey[0];
-    const int cell = D.base + i * D.ny + j;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const float fp = S.f[k][w], fm = S.f[4 + k][w], hp = S.f[8 + k][w], hm = S.f[12 + k][w];
-        float ah = Ph[k], al = Pl[k], th, tl;
+        const float2 fp = S.f[k][r][c], fm = S.f[4 + k][r][c], hp = S.f[8 + k][r][c], hm = S.f[12 + k][r][c];
+        float2 ah = Ph[k], al = Pl[k];
+        auto lam = [&](float2 lh, float2 ll, float2 x, float2& th, float2& tl) {
+            th = mul2(lh, x);
+            tl = LAM_POW2 ? f2(0.f) : add2(fma2(lh, x, neg2(th)), mul2(ll, x));
+        };
+        auto acc = [&](float2 th, float2 tl) {   // (ah, al) += (th, tl)
+            two_sum_acc2(ah, al, th);
+            if (!LAM_POW2) al = add2(al, tl);
+        };
+        float2 th, tl;
         // x west
         if (i > 0) {
-            const float Dw = __fadd_rn(S.f[k][wW], fm);
-            lam_mul<LAM_POW2>(lxh, lxl, Dw, th, tl);
-            two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl);
-            if (li == 0) { float* r = exo[D.ex_base + (i / TI - 1) * D.ny + j].r[1][k]; ff_add(S.lf[0][k][0], S.lf[0][k][1], th, tl, r[0], r[1]); }
+            lam(lx2, lxl2, add2(S.f[k][r - 1][c], fm), th, tl);
+            acc(th, tl);
+            if (r == 1) {   // the tile's west edge: record the full flux this tile applied
+                Edge* e = exo + D.ex_base + (i / TI - 1) * D.ny + jx;
+                ff_add(S.lf[0][k][0], S.lf[0][k][1], th.x, tl.x, e[0].r[1][k][0], e[0].r[1][k][1]);
+                if (has_y) ff_add(S.lf[0][k][0], S.lf[0][k][1], th.y, tl.y, e[1].r[1][k][0], e[1].r[1][k][1]);
+            }
         } else {
-            two_sum_acc(ah, al, S.wc[0][k][0]); al = __fadd_rn(al, S.wc[0][k][1]);
-            if (k == 1) { lam_mul<LAM_POW2>(lxh, lxl, __fmul_rn(2.f, fm), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
+            two_sum_acc2(ah, al, f2(S.wc[0][k][0]));   // wall constant: a full FP32 pair
+            al = add2(al, f2(S.wc[0][k][1]));
+            if (k == 1) { lam(lx2, lxl2, mul2(f2(2.f), fm), th, tl); acc(th, tl); }
         }
         // x east
         if (i < D.nx - 1) {
-            const float De = __fadd_rn(fp, S.f[4 + k][wE]);
-            lam_mul<LAM_POW2>(lxh, lxl, De, th, tl);
-            two_sum_acc(ah, al, -th); if (!LAM_POW2) al = __fadd_rn(al, -tl);
-            if (li == hi_i - 1) { float* r = exo[D.ex_base + ((i + 1) / TI - 1) * D.ny + j].r[0][k]; ff_add(S.lf[0][k][0], S.lf[0][k][1], th, tl, r[0], r[1]); }
+            lam(lx2, lxl2, add2(fp, S.f[4 + k][r + 1][c]), th, tl);
+            acc(neg2(th), neg2(tl));
+            if (r == hi_i) {
+                Edge* e = exo + D.ex_base + ((i + 1) / TI - 1) * D.ny + jx;
+                ff_add(S.lf[0][k][0], S.lf[0][k][1], th.x, tl.x, e[0].r[0][k][0], e[0].r[0][k][1]);
+                if (has_y) ff_add(S.lf[0][k][0], S.lf[0][k][1], th.y, tl.y, e[1].r[0][k][0], e[1].r[0][k][1]);
+            }
         } else {
-            two_sum_acc(ah, al, S.wc[1][k][0]); al = __fadd_rn(al, S.wc[1][k][1]);
-            if (k == 1) { lam_mul<LAM_POW2>(lxh, lxl, -__fmul_rn(2.f, fp), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
+            two_sum_acc2(ah, al, f2(S.wc[1][k][0]));
+            al = add2(al, f2(S.wc[1][k][1]));
+            if (k == 1) { lam(lx2, lxl2, mul2(f2(-2.f), fp), th, tl); acc(th, tl); }
         }
-        // y south
-        if (j > 0) {
-            const float Ds = __fadd_rn(S.f[8 + k][wS], hm);
-            lam_mul<LAM_POW2>(lyh, lyl, Ds, th, tl);
-            two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl);
-            if (lj == 0) { float* r = eyo[D.ey_base + (j / TJ - 1) * D.nx + i].r[1][k]; ff_add(S.lf[1][k][0], S.lf[1][k][1], th, tl, r[0], r[1]); }
-        } else {
-            two_sum_acc(ah, al, S.wc[2][k][0]); al = __fadd_rn(al, S.wc[2][k][1]);
-            if (k == 2) { lam_mul<LAM_POW2>(lyh, lyl, __fmul_rn(2.f, hm), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
+        // y south: lanes (jx-1 | jx) and (jx | jx+1)
+        {
+            const float hpS = S.f[8 + k][r][c - 1].y;
+            lam(ly2, lyl2, add2(make_float2(hpS, hp.x), hm), th, tl);
+            th = mul2(th, mS); tl = mul2(tl, mS);
+            acc(th, tl);
+            if (jx == j0 && j0 > 0) {   // the tile's south edge (lane x)
+                float* rr = eyo[D.ey_base + (j0 / TJ - 1) * D.nx + i].r[1][k];
+                ff_add(S.lf[1][k][0], S.lf[1][k][1], th.x, tl.x, rr[0], rr[1]);
+            }
         }
-        // y north
-        if (j < D.ny - 1) {
-            const float Dn = __fadd_rn(hp, S.f[12 + k][wN]);
-            lam_mul<LAM_POW2>(lyh, lyl, Dn, th, tl);
-            two_sum_acc(ah, al, -th); if (!LAM_POW2) al = __fadd_rn(al, -tl);
-            if (lj == hi_j - 1) { float* r = eyo[D.ey_base + ((j + 1) / TJ - 1) * D.nx + i].r[0][k]; ff_add(S.lf[1][k][0], S.lf[1][k][1], th, tl, r[0], r[1]); }
-        } else {
-            two_sum_acc(ah, al, S.wc[3][k][0]); al = __fadd_rn(al, S.wc[3][k][1]);
-            if (k == 2) { lam_mul<LAM_POW2>(lyh, lyl, -__fmul_rn(2.f, hp), th, tl); two_sum_acc(ah, al, th); if (!LAM_POW2) al = __fadd_rn(al, tl); }
+        // y north: lanes (jx | jx+1) and (jx+1 | jx+2)
+        {
+            const float hmN = S.f[12 + k][r][c + 1].x;
+            lam(ly2, lyl2, add2(hp, make_float2(hm.y, hmN)), th, tl);
+            th = mul2(th, mN); tl = mul2(tl, mN);
+            acc(neg2(th), neg2(tl));
+            const int jn = j0 + hi_j - 1;   // the tile's north edge column
+            if (jn + 1 < D.ny && (jx == jn || jx + 1 == jn)) {
+                const int q = jx == jn ? 0 : 1;
+                float* rr = eyo[D.ey_base + ((jn + 1) / TJ - 1) * D.nx + i].r[0][k];
+                ff_add(S.lf[1][k][0], S.lf[1][k][1], lane(th, q), lane(tl, q), rr[0], rr[1]);
+            }
         }
-        pho[k * P + cell] = ah;
-        plo[k * P + cell] = al;
+        // y walls
+        if (wS || wNx || wNy) {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const bool south = q == 0 && wS, north = q == 0 ? wNx : wNy;
+                if (!south && !north) continue;
+                float h = lane(ah, q), l = lane(al, q);
+                const int w = south ? 2 : 3;
+                two_sum_acc(h, l, S.wc[w][k][0]); l = __fadd_rn(l, S.wc[w][k][1]);
+                if (k == 2) {   // +2 lam_y dhm2 (south), -2 lam_y dhp2 (north)
+                    const float v = south ? __fmul_rn(2.f, lane(hm, q)) : __fmul_rn(-2.f, lane(hp, q));
+                    const float vh = __fmul_rn(D.lyh, v);
+                    const float vl = LAM_POW2 ? 0.f : __fadd_rn(__fmaf_rn(D.lyh, v, -vh), __fmul_rn(D.lyl, v));
+                    two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
+                }
+                set_lane(ah, q, h); set_lane(al, q, l);
+            }
+        }
+        const int cell = D.base + i * D.ny + jx;
+        pho[k * P + cell] = ah.x;
+        plo[k * P + cell] = al.x;
+        if (has_y) {
+            pho[k * P + cell + 1] = ah.y;
+            plo[k * P + cell + 1] = al.y;
+        }
     }
 }
 
@@ -684,11 +822,11 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
         A.step = (int)st;
         A.s0 = s0;
         if (kahan) {
-            if (pow2) k_step2d<true, true><<<ntiles, NT, 0, s>>>(A);
-            else k_step2d<true, false><<<ntiles, NT, 0, s>>>(A);
+            if (pow2) k_step2d<true, true><<<ntiles, NTP, 0, s>>>(A);
+            else k_step2d<true, false><<<ntiles, NTP, 0, s>>>(A);
         } else {
-            if (pow2) k_step2d<false, true><<<ntiles, NT, 0, s>>>(A);
-            else k_step2d<false, false><<<ntiles, NT, 0, s>>>(A);
+            if (pow2) k_step2d<false, true><<<ntiles, NTP, 0, s>>>(A);
+            else k_step2d<false, false><<<ntiles, NTP, 0, s>>>(A);
         }
         launches++;
         if (st + 1 - s0 == d->fold || st + 1 == maxsteps) {

@@ -113,6 +113,9 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(fast_rcp(a.x), fast_rcp(a.y)); }
 __device__ __forceinline__ float2 rsqrt2(float2 a) { return make_float2(rsqrtf(a.x), rsqrtf(a.y)); }
+// lane q of a float2 (q a compile-time constant after unrolling)
+__device__ __forceinline__ float lane(float2 v, int q) { return q ? v.y : v.x; }
+__device__ __forceinline__ void set_lane(float2& v, int q, float x) { if (q) v.y = x; else v.x = x; }
 
 // h + l += v per lane (TwoSum)
 __device__ __forceinline__ void two_sum_acc2(float2& h, float2& l, float2 v) {
