@@ -189,8 +189,9 @@ def describe(workload, cells, order):
 class Problem:
     """One workload instance on the GPU: single context or batch, with reset + timed run."""
 
-    def __init__(self, shll, workload, precision, cells, order, fold, stream):
+    def __init__(self, shll, workload, precision, cells, order, fold, stream, tune=True):
         self.shll, self.workload, self.stream = shll, workload, stream
+        self.precision, self.tune, self.tuned = precision, tune and not fold, False
         self.batch = workload.startswith("batch")
         self.dim = 2 if workload in ("circle2d", "batch2d") else 1
         if self.batch:
@@ -218,7 +219,23 @@ class Problem:
             self.obj.init_state()
         self.obj.set_stream(self.stream.cuda_stream)
         if self.dim == 1:
+            if self.tune and self.precision.startswith("mixed") and not self.tuned:
+                self.obj.autotune()   # untimed: sweep length and fold window per size class
+                self.tuned = True
             self.obj.checkpoint()
+
+    def tuning(self):
+        """The autotuner's choices: {"sweep_steps/fold_steps": items}."""
+        if self.dim != 1 or not self.precision.startswith("mixed"):
+            return None
+        if not self.batch:
+            b, f = self.obj.tuning()
+            return {f"{b}/{f}": 1}
+        out = {}
+        for i in range(len(self.items)):
+            b, f = self.obj.tuning(i)
+            out[f"{b}/{f}"] = out.get(f"{b}/{f}", 0) + 1
+        return out
 
     def reset_from_host(self):
         """Rebuilds the problem from host data (the end-to-end leg: descriptors and initial state
@@ -307,6 +324,7 @@ def main():
     ap.add_argument("--fold", type=int, default=0, help="fold interval of the mixed path (0 = library default)")
     ap.add_argument("--precision", default="mixed_f64")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison runs and CPU baseline")
+    ap.add_argument("--no-tune", action="store_true", help="1D mixed: skip the autotuner (library defaults)")
     args = ap.parse_args()
     workload = args.workload
     if args.cells == 0:
@@ -341,7 +359,7 @@ def main():
         dist.init_process_group("nccl")
     shll = load_pkg()
     stream = torch.cuda.Stream()
-    prob = Problem(shll, workload, args.precision, args.cells, args.order, args.fold, stream)
+    prob = Problem(shll, workload, args.precision, args.cells, args.order, args.fold, stream, tune=not args.no_tune)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     for _ in range(W):
         prob.reset()
@@ -417,7 +435,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64"
             else args.precision, "data": "synthetic",
             "config": dict(config, cell_updates_per_run=prob.cu, precision=args.precision,
-                           fold_steps=args.fold or (64 if prob.dim == 1 else 16), parallelism=f"replicas{world}",
+                           fold_steps=args.fold or ("autotuned" if prob.tuning() else (64 if prob.dim == 1 else 16)),
+                           tuning=prob.tuning(),
+                           parallelism=f"replicas{world}",
                            l2="flushed between runs (256 MB write)"),
             "roofline": roofline,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,

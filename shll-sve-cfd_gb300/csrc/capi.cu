@@ -466,6 +466,20 @@ extern "C" int shll_run(shll_ctx* c, long* steps_taken) {
     return rc;
 }
 
+extern "C" int shll_autotune(shll_ctx* c, int trial_steps) {
+    if (!c) return SHLL_ERR_ARG;
+    if (c->plain || c->p.dim != 1) { set_err(c, "the autotuner covers the mixed 1D engine"); return SHLL_ERR_UNSUPPORTED; }
+    if (!c->initialized) { set_err(c, "state not initialised (call shll_init_state)"); return SHLL_ERR_STATE; }
+    int rc = mixed_autotune(c->mixed, trial_steps, c->err, sizeof(c->err));
+    if (rc == SHLL_OK) c->ck_steps = c->steps_taken;   // the device checkpoint now holds this state
+    return rc;
+}
+
+extern "C" int shll_tuning(shll_ctx* c, int* sweep_steps, int* fold_steps) {
+    if (!c || c->plain || c->p.dim != 1) return SHLL_ERR_ARG;
+    return mixed_tuning(c->mixed, 0, sweep_steps, fold_steps);
+}
+
 extern "C" long shll_steps_taken(const shll_ctx* c) { return c ? c->steps_taken : -1; }
 
 static std::atomic<long> g_launches{0};
@@ -756,6 +770,18 @@ extern "C" long shll_batch_cell_updates(const shll_batch* b) {
     return b->pb ? plain_batch_cell_updates(b->pb) : mixed_cell_updates(b->m);
 }
 extern "C" const char* shll_batch_last_error(const shll_batch* b) { return b ? b->err : "no batch"; }
+
+// autotuner of the mixed 1D engine (state restored afterwards) and its choices per item
+extern "C" int shll_batch_autotune(shll_batch* b, int trial_steps) {
+    if (!b) return SHLL_ERR_ARG;
+    if (!b->m) { snprintf(b->err, sizeof(b->err), "the autotuner needs a mixed-precision batch"); return SHLL_ERR_UNSUPPORTED; }
+    return mixed_autotune(b->m, trial_steps, b->err, sizeof(b->err));
+}
+
+extern "C" int shll_batch_tuning(shll_batch* b, int item, int* sweep_steps, int* fold_steps) {
+    if (!b || !b->m || item < 0 || item >= b->count) return SHLL_ERR_ARG;
+    return mixed_tuning(b->m, item, sweep_steps, fold_steps);
+}
 
 // device-side checkpoint / restore of a mixed-precision 1D batch (restore also clears the
 // breakdown flags raised after the checkpoint)

@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -55,7 +56,9 @@ struct TubeP {
     float alpha;
     float gRf, Rf, cvinvf;  // gamma R, R, 1/CV in FP32
     int lam_pow2;     // lam is a power of two: lam*Delta is exact in FP32
+    int B;            // steps per sweep (temporal blocking depth, <= MW / 16)
     int fold_sweeps;  // sweeps per fold window (FP64 state read at the first, written at the last)
+    int owned;        // owned cells per chunk (0: the window minus the halos)
 };
 
 struct Chunk {
@@ -143,7 +146,7 @@ struct SweepArgs {
     float* dl[2];
     Frame1* frames;     // per chunk id: the frame of the current fold window
     long plane;         // cells per plane (all tubes)
-    int sweep, B;
+    int sweep;
     int chunk0;         // first chunk of the launch (chunks are grouped by scheme variant)
     int* flag;
     int* item_flags;    // per tube (may be null)
@@ -183,7 +186,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
 
     const int tid = threadIdx.x;
     const int n = tp.n;
-    const int steps = min(A.B, tp.steps - A.sweep * A.B);
+    const int steps = min(tp.B, tp.steps - A.sweep * tp.B);
     if (steps <= 0) return;
     const int H = R_ * steps;
     const int ws = max(0, ch.a - H), we = min(n, ch.b + H), L = we - ws;
@@ -193,7 +196,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     // the last one writes the state back; the sweeps between exchange deviation pairs
     const int F = tp.fold_sweeps;
     const int jw = A.sweep % F;
-    const int nsw = (tp.steps + A.B - 1) / A.B;
+    const int nsw = (tp.steps + tp.B - 1) / tp.B;
     const bool wstart = jw == 0;
     const bool wend = jw == F - 1 || A.sweep == nsw - 1;
     // (selects rather than indexing the parameter arrays, which would copy them to local memory)
@@ -206,7 +209,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     const double lam = tp.lam;
     const float lamh = (float)lam, laml = (float)(lam - (double)lamh);
 
-    if (L > MW || A.B > MW / 16) {  // host guarantees this never happens; refuse rather than overrun
+    if (L > MW || tp.B > MW / 16 || tp.B < 1) {  // host guarantees this never happens; refuse rather than overrun
         if (tid == 0) atomicOr(A.flag, SHLL_FLAG_BADARG);
         return;
     }
@@ -636,7 +639,7 @@ __global__ void k_fixup1d(SweepArgs A, int nchunks) {
     const Chunk ch = A.chunks[c];
     const TubeP tp = A.tubes[ch.tube];
     if (ch.idL < 0 || tp.steps <= 0) return;
-    const int sweeps = (tp.steps + A.B - 1) / A.B;
+    const int sweeps = (tp.steps + tp.B - 1) / tp.B;
     const BSum* bs = ((sweeps - 1) & 1) ? A.bsum[1] : A.bsum[0];
     const int buf = (tp.par + sweeps) & 1;
     for (int k = 0; k < 3; k++) {
@@ -686,6 +689,7 @@ struct MixedState {
     };
     std::vector<GraphEntry> graphs;
     std::vector<std::pair<std::vector<long>, std::vector<int>>> seen;  // runs launched once so far
+    bool tuning = false;               // autotuner trials: launch directly, no capture
     long cell_updates = 0;
     // device checkpoint (shll_checkpoint)
     void* ck_hi[2] = {nullptr, nullptr};
@@ -696,15 +700,42 @@ struct MixedState {
     void* d2 = nullptr;
 };
 
-// owned cells per chunk: the window (MW) minus the halo on both sides; SHLL_MIXED_CHUNK (cells)
-// may lower it to put more CTAs on each SM
-static int chunk_owned(int order, int B) {
-    int S = MW - 2 * order * B;
-    if (const char* e = getenv("SHLL_MIXED_CHUNK")) {
-        int v = atoi(e);
-        if (v >= 4 * order * B && v < S) S = v;
+// ---- autotuner choices, process-wide, by size class ----
+// A class is (order, limiter, lam a power of two, state format, floor(log2(cells))); its choice is
+// the sweep length B, the sweeps per fold window and the owned cells per chunk (0: the largest).
+struct TuneKey {
+    int order, limiter, pow2, kahan, lg;
+    bool operator<(const TuneKey& o) const {
+        if (order != o.order) return order < o.order;
+        if (limiter != o.limiter) return limiter < o.limiter;
+        if (pow2 != o.pow2) return pow2 < o.pow2;
+        if (kahan != o.kahan) return kahan < o.kahan;
+        return lg < o.lg;
     }
-    return S;
+};
+struct TuneVal { int B, fold_sweeps, owned; };
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneVal> g_tune;
+
+static TuneKey tune_key(const TubeP& tp, bool kahan) {
+    int lg = 0;
+    while ((2 << lg) <= tp.n) lg++;
+    return {tp.order, tp.order == 2 ? tp.limiter : 0, tp.lam_pow2, kahan ? 1 : 0, lg};
+}
+static void apply_tuning(TubeP& tp, bool kahan) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(tp, kahan));
+    if (it == g_tune.end()) return;
+    tp.B = it->second.B;
+    tp.fold_sweeps = it->second.fold_sweeps;
+    tp.owned = it->second.owned;
+}
+
+// owned cells per chunk: the window (MW) minus the halo on both sides, or the tube's tuned
+// smaller size
+static int chunk_owned(const TubeP& tp) {
+    const int S = MW - 2 * tp.order * tp.B;
+    return tp.owned > 0 && tp.owned < S ? tp.owned : S;
 }
 
 // Chunks of every tube.  A tube has at least two chunks; the first chunk's frame is anchored
@@ -716,7 +747,7 @@ static void build_chunks(MixedState* m) {
     for (int t = 0; t < m->nitems; t++) {
         const TubeP& tp = m->tubes[t];
         const int n = tp.n;
-        const int S = chunk_owned(tp.order, m->B);
+        const int S = chunk_owned(tp);
         int k = n <= MW ? 2 : (n + S - 1) / S;
         if (k > n) k = n;
         std::vector<int> edges(k + 1), anc(k);
@@ -727,6 +758,14 @@ static void build_chunks(MixedState* m) {
             m->chunks.push_back({t, edges[c], edges[c + 1], anc[c], id0 + c, c > 0 ? id0 + c - 1 : -1,
                                  c + 1 < k ? id0 + c + 1 : -1});
     }
+}
+
+// fold windows of several sweeps need every halo cell to come from the adjacent chunk
+static void fix_fold_sweeps(MixedState* m) {
+    std::vector<int> min_owned(m->nitems, 1 << 30);
+    for (const Chunk& c : m->chunks) min_owned[c.tube] = std::min(min_owned[c.tube], c.b - c.a);
+    for (int t = 0; t < m->nitems; t++)
+        if (min_owned[t] < m->tubes[t].order * m->tubes[t].B) m->tubes[t].fold_sweeps = 1;
 }
 
 static int alloc_mixed(MixedState* m, char* err, size_t len) {
@@ -859,17 +898,17 @@ MixedState* mixed_create_batch(const shll_params* items, int count, cudaStream_t
     long off = 0;
     for (int t = 0; t < count; t++) {
         const shll_params& p = items[t];
-        m->tubes.push_back(tube_params(p, off));
+        TubeP tp = tube_params(p, off);
+        tp.B = m->B;
+        tp.fold_sweeps = fold_sweeps;
+        if (items[t].fold_steps <= 0) apply_tuning(tp, m->kahan);   // a tuned choice of this size class
+        m->tubes.push_back(tp);
         off += p.nx;
     }
     m->plane = off;
     m->par.assign(count, 0);
     build_chunks(m);
-    // windows of several sweeps need every halo cell to come from the adjacent chunk
-    std::vector<int> min_owned(count, 1 << 30);
-    for (const Chunk& c : m->chunks) min_owned[c.tube] = std::min(min_owned[c.tube], c.b - c.a);
-    for (int t = 0; t < count; t++)
-        m->tubes[t].fold_sweeps = min_owned[t] >= m->tubes[t].order * m->B ? fold_sweeps : 1;
+    fix_fold_sweeps(m);
     int rc = alloc_mixed(m, err, len);
     if (rc == SHLL_OK && cudaMalloc(&m->d_chunks, sizeof(Chunk) * m->chunks.size()) != cudaSuccess) rc = SHLL_ERR_NOMEM;
     if (rc != SHLL_OK) {
@@ -982,7 +1021,7 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
         const int v = tube_variant(tp);
         if (groups.empty() || groups.back().variant != v) groups.push_back({v, c, std::vector<int>(nsweeps + 1, 0)});
         // active[k] = chunks of the group whose tube still has sweep k (suffix sum of a histogram)
-        groups.back().active[(tp.steps + m->B - 1) / m->B]++;
+        groups.back().active[(tp.steps + tp.B - 1) / tp.B]++;
     }
     for (Group& g : groups)
         for (long k = nsweeps - 1; k >= 0; k--) g.active[k] += g.active[k + 1];
@@ -996,7 +1035,6 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
     A.dl[0] = m->dl[0]; A.dl[1] = m->dl[1];
     A.frames = m->frames;
     A.plane = m->plane;
-    A.B = m->B;
     A.flag = m->d_flag;
     A.item_flags = m->d_item_flags;
     A.sweep = 0;
@@ -1038,22 +1076,24 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     // chunks grouped by scheme variant and, inside a group, ordered by their tube's sweep count,
     // so that the launch of sweep k for a group covers a prefix of the group
     std::vector<Chunk> order = m->chunks;
+    auto sweeps_of = [&](const TubeP& tp) { return (tp.steps + tp.B - 1) / tp.B; };
     std::stable_sort(order.begin(), order.end(), [&](const Chunk& x, const Chunk& y) {
         const int vx = tube_variant(m->tubes[x.tube]), vy = tube_variant(m->tubes[y.tube]);
         if (vx != vy) return vx < vy;
-        return m->tubes[x.tube].steps > m->tubes[y.tube].steps;
+        return sweeps_of(m->tubes[x.tube]) > sweeps_of(m->tubes[y.tube]);
     });
     if (cudaMemcpyAsync(m->d_tubes, m->tubes.data(), sizeof(TubeP) * m->nitems, cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
         cudaMemcpyAsync(m->d_chunks, order.data(), sizeof(Chunk) * order.size(), cudaMemcpyHostToDevice, m->stream) != cudaSuccess) {
         snprintf(err, len, "descriptor upload failed");
         return SHLL_ERR_CUDA;
     }
-    const long nsweeps = (maxsteps + m->B - 1) / m->B;
+    long nsweeps = 0;
+    for (const TubeP& tp : m->tubes) nsweeps = std::max(nsweeps, (long)sweeps_of(tp));
     long launches = 0;
     cudaError_t e = allow_solo_padding();
     if (e != cudaSuccess) { snprintf(err, len, "kernel attribute: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     MixedState::GraphEntry* hit = nullptr;
-    const bool replay = g_graph_replay.load() != 0;
+    const bool replay = g_graph_replay.load() != 0 && !m->tuning;
     if (replay)
         for (auto& g : m->graphs)
             if (g.steps == steps && g.par == m->par) hit = &g;
@@ -1093,10 +1133,134 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     if (e != cudaSuccess) { snprintf(err, len, "sweep launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     shll_count_launches(launches);
     for (int t = 0; t < m->nitems; t++) {
-        long sw = (steps[t] + m->B - 1) / m->B;
+        long sw = (steps[t] + m->tubes[t].B - 1) / m->tubes[t].B;
         m->par[t] = (int)((m->par[t] + sw) & 1);
         m->cell_updates += steps[t] * (long)m->tubes[t].n;
     }
+    return SHLL_OK;
+}
+
+// re-chunks every tube after a change of sweep lengths or chunk sizes (descriptors, boundary
+// sums, frame table; captured launch sequences are dropped)
+static int rebuild_chunks(MixedState* m, char* err, size_t len) {
+    for (TubeP& tp : m->tubes) tp.fold_sweeps = std::max(tp.fold_sweeps, 1);
+    build_chunks(m);
+    fix_fold_sweeps(m);
+    for (auto& g : m->graphs) cudaGraphExecDestroy(g.exec);
+    m->graphs.clear();
+    m->seen.clear();
+    const size_t nch = m->chunks.size();
+    cudaFree(m->d_chunks); m->d_chunks = nullptr;
+    cudaFree(m->frames); m->frames = nullptr;
+    for (int b = 0; b < 2; b++) { cudaFree(m->bsum[b]); m->bsum[b] = nullptr; }
+    bool ok = cudaMalloc(&m->d_chunks, sizeof(Chunk) * nch) == cudaSuccess &&
+              cudaMalloc(&m->frames, sizeof(Frame1) * nch) == cudaSuccess &&
+              cudaMalloc(&m->bsum[0], sizeof(BSum) * nch) == cudaSuccess &&
+              cudaMalloc(&m->bsum[1], sizeof(BSum) * nch) == cudaSuccess;
+    bool windows = false;
+    for (const TubeP& tp : m->tubes) windows = windows || tp.fold_sweeps > 1;
+    const size_t cells = (size_t)m->plane * 3;
+    for (int b = 0; ok && windows && b < 2; b++)
+        if (!m->dh[b])
+            ok = cudaMalloc(&m->dh[b], cells * sizeof(float)) == cudaSuccess &&
+                 cudaMalloc(&m->dl[b], cells * sizeof(float)) == cudaSuccess;
+    if (!ok) { snprintf(err, len, "re-chunking allocation failed"); return SHLL_ERR_NOMEM; }
+    return SHLL_OK;
+}
+
+// Autotuner: picks, per size class, the sweep length B (the temporal-blocking depth, which sets a
+// chunk's owned and halo cells) and the sweeps per FP64 fold window by timing short runs of this
+// batch.  The state is checkpointed first and restored after every trial; the choices are kept
+// in the process-wide table, so later batches and tubes of the same classes start with them.
+int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
+    if (m->dim != 1) { snprintf(err, len, "the autotuner covers the 1D engine"); return SHLL_ERR_UNSUPPORTED; }
+    long cells = 0;
+    double work_total = 0;
+    for (const TubeP& tp : m->tubes) { cells += tp.n; work_total += (double)tp.n * tp.n; }
+    if (trial_steps <= 0) {  // about 4e8 cell-updates per trial, whole fold windows of up to 128 steps
+        const long want = (long)(4e8 / (double)std::max(cells, 1L));
+        trial_steps = (int)std::min(4096L, std::max(256L, (want + 255) / 256 * 256));
+    }
+    int rc = mixed_checkpoint(m, false, err, len);
+    if (rc != SHLL_OK) return rc;
+    m->tuning = true;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const std::vector<long> steps(m->nitems, trial_steps);
+    // time of one trial: best of two runs from the checkpoint
+    auto trial = [&](float* ms) -> int {
+        int r = rebuild_chunks(m, err, len);
+        float best = 1e30f;
+        for (int rep = 0; r == SHLL_OK && rep < 2; rep++) {
+            r = mixed_checkpoint(m, true, err, len);
+            if (r != SHLL_OK) break;
+            cudaEventRecord(e0, m->stream);
+            r = run_tubes(m, steps, err, len);
+            cudaEventRecord(e1, m->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { snprintf(err, len, "trial failed"); r = SHLL_ERR_CUDA; }
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            best = std::min(best, t);
+        }
+        *ms = best;
+        return r;
+    };
+    struct Cand { int B, F; };
+    std::vector<Cand> cands;
+    for (int B : {8, 16, 32})
+        for (int F : {1, 2, 4, 8})
+            if (B * F <= std::max(trial_steps, 128) && B <= MW / 16) cands.push_back({B, F});
+    std::map<TuneKey, std::vector<int>> classes;
+    for (int t = 0; t < m->nitems; t++) classes[tune_key(m->tubes[t], m->kahan)].push_back(t);
+    auto set_class = [&](const std::vector<int>& ts, Cand c) {
+        for (int t : ts) { m->tubes[t].B = c.B; m->tubes[t].fold_sweeps = c.F; m->tubes[t].owned = 0; }
+    };
+    // 1) one choice for every class
+    Cand best_all = {m->B, 1};
+    float best_ms = 1e30f;
+    for (const Cand& c : cands) {
+        for (auto& kv : classes) set_class(kv.second, c);
+        float ms = 0;
+        rc = trial(&ms);
+        if (rc != SHLL_OK) break;
+        if (ms < best_ms) { best_ms = ms; best_all = c; }
+    }
+    std::map<TuneKey, Cand> choice;
+    for (auto& kv : classes) { set_class(kv.second, best_all); choice[kv.first] = best_all; }
+    // 2) the classes that hold at least a tenth of the work, one at a time
+    for (auto& kv : classes) {
+        if (rc != SHLL_OK) break;
+        double w = 0;
+        for (int t : kv.second) w += (double)m->tubes[t].n * m->tubes[t].n;
+        if (w < 0.1 * work_total || classes.size() == 1) continue;
+        for (const Cand& c : cands) {
+            if (c.B == choice[kv.first].B && c.F == choice[kv.first].F) continue;
+            set_class(kv.second, c);
+            float ms = 0;
+            rc = trial(&ms);
+            if (rc != SHLL_OK) break;
+            if (ms < 0.99f * best_ms) { best_ms = ms; choice[kv.first] = c; }
+        }
+        set_class(kv.second, choice[kv.first]);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->tuning = false;
+    if (rc == SHLL_OK) rc = rebuild_chunks(m, err, len);
+    if (rc == SHLL_OK) rc = mixed_checkpoint(m, true, err, len);
+    if (rc != SHLL_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto& kv : choice) g_tune[kv.first] = {kv.second.B, kv.second.F, 0};
+    return SHLL_OK;
+}
+
+// sweep length and fold interval (steps) chosen for a tube
+int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps) {
+    if (m->dim != 1 || item < 0 || item >= m->nitems) return SHLL_ERR_ARG;
+    const TubeP& tp = m->tubes[item];
+    if (sweep_steps) *sweep_steps = tp.B;
+    if (fold_steps) *fold_steps = tp.B * tp.fold_sweeps;
     return SHLL_OK;
 }
 
@@ -1329,11 +1493,13 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     const int fold = p->fold_steps > 0 ? p->fold_steps : kSweepSteps;
     const int B = std::min(fold, MW / 16);
     TubeP tp = tube_params(*p, 0);
+    tp.B = B;
+    tp.fold_sweeps = 1;
     tp.steps = (int)nsteps;
     tp.par = 0;
     Chunk chunks[kStaticMaxChunks];
     const int n = tp.n;
-    const int S = chunk_owned(tp.order, B);
+    const int S = chunk_owned(tp);
     int k = n <= MW ? 2 : (n + S - 1) / S;
     if (k > n) k = n;
     if (k > kStaticMaxChunks) {
@@ -1366,7 +1532,6 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.bsum[0] = reinterpret_cast<BSum*>(sc + kStaticBSumOff);
     A.bsum[1] = A.bsum[0] + kStaticMaxChunks;
     A.plane = n;
-    A.B = B;
     A.flag = d_flag;
     A.item_flags = nullptr;
     A.chunk0 = 0;

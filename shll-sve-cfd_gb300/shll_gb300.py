@@ -56,7 +56,7 @@ EXPORTS = [
     "Compute_U_from_P", "Compute_P_from_U", "Compute_F_from_P", "Update_U_from_F", "Save_Results",
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
     "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
-    "shll_batch_restore",
+    "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
 ]
 
 
@@ -242,6 +242,15 @@ class Context:
         self._ck(lib().shll_totals(self.h, _dp(out)), "totals")
         return out
 
+    def autotune(self, trial_steps=0):
+        """Picks sweep length and fold window by timed trials (mixed 1D; state restored)."""
+        return self._ck(lib().shll_autotune(self.h, trial_steps), "autotune")
+
+    def tuning(self):
+        b, f = ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().shll_tuning(self.h, ctypes.byref(b), ctypes.byref(f)), "tuning")
+        return b.value, f.value
+
     def checkpoint(self):
         return self._ck(lib().shll_checkpoint(self.h), "checkpoint")
 
@@ -278,6 +287,16 @@ class Batch:
             return rc
         self._ck(rc, "batch_run")
         return rc
+
+    def autotune(self, trial_steps=0):
+        """Picks sweep length and fold window per size class by timed trials (state restored)."""
+        return self._ck(lib().shll_batch_autotune(self.h, trial_steps), "batch_autotune")
+
+    def tuning(self, i):
+        """(sweep length, fold interval) in steps chosen for item i."""
+        b, f = ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().shll_batch_tuning(self.h, i, ctypes.byref(b), ctypes.byref(f)), "batch_tuning")
+        return b.value, f.value
 
     def checkpoint(self):
         """Device-side copy of the state (mixed-precision 1D batches)."""

@@ -120,3 +120,35 @@ def test_repeated_run_replays_identically(shll):
     c.run()
     assert np.array_equal(c.primitives(), first)
     assert shll.kernel_launches() - n1 > 100   # the replay counts its launches too
+
+
+def test_autotune_batch_keeps_results_and_conservation(shll, oracle):
+    # First-order tubes of several size classes: after tuning, a run still matches the FP64 oracle
+    # to 1e-6 and conserves mass to FP64 rounding; the choices are in the candidate set and a new
+    # batch of the same classes starts with them.
+    sizes = [300, 700, 1500, 3000, 6000, 3000, 1500, 700]
+    items = [shll.params(1, 1, nx=n, precision="mixed_f64") for n in sizes]
+    b = shll.Batch(items)
+    t0 = [b.totals(i)[0] for i in range(len(items))]
+    b.autotune(256)
+    chosen = [b.tuning(i) for i in range(len(items))]
+    for sweep, fold in chosen:
+        assert sweep in (8, 16, 32) and fold % sweep == 0 and fold // sweep in (1, 2, 4, 8)
+    b.run()
+    for i, n in enumerate(sizes):
+        _, ref, _ = oracle.run(oracle.make_cfg(order=1, nx=n), oracle.ic_sod(n))
+        assert np.max(np.mean(np.abs(b.primitives(i) - ref), axis=1)) <= 1e-6, n
+        assert abs(b.totals(i)[0] - t0[i]) / t0[i] <= 1e-12
+    b2 = shll.Batch([shll.params(1, 1, nx=n, precision="mixed_f64") for n in sizes])
+    assert [b2.tuning(i) for i in range(len(items))] == chosen
+
+
+def test_autotune_single_tube(shll, oracle):
+    c = shll.Context(shll.params(1, 2, nx=1024, precision="mixed_f64"))
+    c.init_state()
+    c.autotune(256)
+    sweep, fold = c.tuning()
+    assert sweep in (8, 16, 32)
+    c.run()
+    _, ref, _ = oracle.run(oracle.make_cfg(order=2, nx=1024), oracle.ic_sod(1024))
+    assert np.max(np.mean(np.abs(c.primitives() - ref), axis=1)) <= 1e-6
