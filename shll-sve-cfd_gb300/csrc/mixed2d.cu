@@ -185,7 +185,7 @@ __device__ __forceinline__ void dflux2(const AnchorCoef& cx, const AnchorCoef& c
 
 // anchor coefficients of a 2D tile frame, each duplicated into both FP32x2 lanes
 struct Coef2D {
-    float2 rho, u, v, nu, nv, ne, T, a, gR, R, cvinv, P, m, n, E;
+    float2 rho, u, v, nu, nv, ne, T, a, gR, R, cvinv, P, m, n, E, gm1;
     float2 Mx, nMx, Z1x, Z2x, My, nMy, Z1y, Z2y;
     float2 Fx[4], Fy[4], Uf[4];
 };
@@ -193,7 +193,7 @@ __device__ __forceinline__ Coef2D coef2d(const AnchorCoef& cx, const AnchorCoef&
     Coef2D k;
     k.rho = f2(cx.rho); k.u = f2(cx.u); k.v = f2(cx.v); k.nu = f2(-cx.u); k.nv = f2(-cx.v); k.ne = f2(-cx.e);
     k.T = f2(cx.T); k.a = f2(cx.a); k.gR = f2(cx.gR); k.R = f2(cx.R); k.cvinv = f2(cx.cvinv); k.P = f2(cx.P);
-    k.m = f2(cx.Uf[1]); k.n = f2(cx.Uf[2]); k.E = f2(cx.Uf[3]);
+    k.m = f2(cx.Uf[1]); k.n = f2(cx.Uf[2]); k.E = f2(cx.Uf[3]); k.gm1 = f2(__fmul_rn(cx.R, cx.cvinv));
     k.Mx = f2(cx.M); k.nMx = f2(-cx.M); k.Z1x = f2(cx.Z1); k.Z2x = f2(cx.Z2);
     k.My = f2(cy.M); k.nMy = f2(-cy.M); k.Z1y = f2(cy.Z1); k.Z2y = f2(cy.Z2);
     for (int q = 0; q < 4; q++) { k.Fx[q] = f2(cx.F[q]); k.Fy[q] = f2(cy.F[q]); k.Uf[q] = f2(cx.Uf[q]); }
@@ -218,7 +218,9 @@ __device__ __forceinline__ void dflux2x2(const Coef2D& c, const float2 d[4], flo
     const float2 ainv = rsqrt2(gRT);
     const float2 a = mul2(gRT, ainv);
     const float2 da = mul2(mul2(c.gR, dT), rcp2(add2(a, c.a)));
-    const float2 dP = mul2(c.R, fma2(drho, T, mul2(c.rho, dT)));
+    // dP = (gamma-1)(dE - (dm u + m* du + dn v + n* dv) / 2): the energy form (see dflux1x2)
+    const float2 dkin = fma2(dm, u, fma2(c.m, du, fma2(dn, v, mul2(c.n, dv))));
+    const float2 dP = mul2(c.gm1, fma2(f2(-0.5f), dkin, dE));
     const float2 P = add2(c.P, dP);
     const float2 EP = add2(add2(c.E, dE), P), dEP = add2(dE, dP);
     {   // x direction, M = u / a

@@ -157,7 +157,7 @@ __device__ __forceinline__ float2 slope2(float2 a, float2 b, float alpha) {
 // anchor coefficients of a 1D frame, each duplicated into both lanes (negated where the
 // formulas subtract them)
 struct Coef2 {
-    float2 rho, u, nu, ne, T, a, M, nM, Z1, Z2, P, gR, R, cvinv;
+    float2 rho, u, nu, ne, T, a, M, nM, Z1, Z2, P, gR, R, cvinv, gm1;
     float2 F[3], Uf[3];
 };
 __device__ __forceinline__ Coef2 coef2(const AnchorCoef& c) {
@@ -166,6 +166,7 @@ __device__ __forceinline__ Coef2 coef2(const AnchorCoef& c) {
     k.M = f2(c.M); k.nM = f2(-c.M); k.Z1 = f2(c.Z1); k.Z2 = f2(c.Z2); k.P = f2(c.P); k.gR = f2(c.gR);
     k.R = f2(c.R);
     k.cvinv = f2(c.cvinv);
+    k.gm1 = f2(__fmul_rn(c.R, c.cvinv));   // R / CV = gamma - 1
     for (int i = 0; i < 3; i++) { k.F[i] = f2(c.F[i]); k.Uf[i] = f2(c.Uf[i]); }
     return k;
 }
@@ -192,7 +193,10 @@ __device__ __forceinline__ void dflux1x2(const Coef2& c, const float2 d[3], floa
     const float2 omm = fma2(neg2(M), M, f2(1.0f));
     const float2 dZ2 = mul2(f2(0.5f), fma2(da, omm, neg2(mul2(mul2(c.a, add2(M, c.M)), dM))));
     const float2 Z2 = add2(c.Z2, dZ2);
-    const float2 dP = mul2(c.R, fma2(drho, T, mul2(c.rho, dT)));
+    // P = (gamma-1)(E - m u / 2): dP = (gamma-1)(dE - (dm u + m* du) / 2).  At a contact (P and u
+    // continuous) this cancels kinetic-energy-sized terms, where R (drho T + rho* dT) would cancel
+    // internal-energy-sized ones
+    const float2 dP = mul2(c.gm1, fma2(f2(-0.5f), fma2(dm, u, mul2(c.Uf[1], du)), dE));
     const float2 P = add2(c.P, dP);
     const float2 E = add2(c.Uf[2], dE);
     float2 dF[3];
