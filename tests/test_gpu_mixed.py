@@ -152,3 +152,19 @@ def test_autotune_single_tube(shll, oracle):
     c.run()
     _, ref, _ = oracle.run(oracle.make_cfg(order=2, nx=1024), oracle.ic_sod(1024))
     assert np.max(np.mean(np.abs(c.primitives() - ref), axis=1)) <= 1e-6
+
+
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+@pytest.mark.parametrize("order,n,cfl,limiter", [(1, 1000, 0.3, 0), (2, 512, 0.3, 0), (2, 512, 0.25, 1), (2, 300, 0.3, 1)])
+def test_mixed_1d_general_lambda_and_mc_limiter(shll, oracle, prec, order, n, cfl, limiter):
+    # lam = cfl / (R + 1) = 0.15 is not a power of two (interface terms carried as FP32 pairs); the
+    # MC limiter of base-omp (alpha 1.25) in the second-order reconstruction
+    prim = oracle.ic_sod(n)
+    cfg = oracle.make_cfg(order=order, nx=n, cfl=cfl, limiter=limiter, mc_alpha=1.25)
+    steps, ref, ref_cons = oracle.run(cfg, prim)
+    s, out, t0, t1 = run_mixed(shll, shll.params(1, order, nx=n, precision=prec, cfl=cfl, limiter=limiter,
+                                                 mc_alpha=1.25))
+    assert s == steps
+    assert np.all(l1(out, ref) <= 1e-6), l1(out, ref)
+    ref_dm = ref_cons[0].sum() - prim[0].sum()
+    assert abs((t1[0] - t0[0]) - ref_dm) / t0[0] <= 1e-12
