@@ -72,16 +72,32 @@ struct Frame2 {
     AnchorCoef cx, cy;               // coefficients for the x and y split fluxes
 };
 
-// What a step needs of its tile's frame, as FP32 values and pairs (written once per fold window by
-// k_tileconst2d, so that no step does FP64 arithmetic)
+// anchor coefficients of a 2D tile frame, each duplicated into both FP32x2 lanes
+struct Coef2D {
+    float2 rho, u, v, nu, nv, ne, T, a, gR, R, cvinv, P, m, n, E, gm1;
+    float2 Mx, nMx, Z1x, Z2x, My, nMy, Z1y, Z2y;
+    float2 Fx[4], Fy[4], Uf[4];
+};
+__device__ __forceinline__ Coef2D coef2d(const AnchorCoef& cx, const AnchorCoef& cy) {
+    Coef2D k;
+    k.rho = f2(cx.rho); k.u = f2(cx.u); k.v = f2(cx.v); k.nu = f2(-cx.u); k.nv = f2(-cx.v); k.ne = f2(-cx.e);
+    k.T = f2(cx.T); k.a = f2(cx.a); k.gR = f2(cx.gR); k.R = f2(cx.R); k.cvinv = f2(cx.cvinv); k.P = f2(cx.P);
+    k.m = f2(cx.Uf[1]); k.n = f2(cx.Uf[2]); k.E = f2(cx.Uf[3]); k.gm1 = f2(__fmul_rn(cx.R, cx.cvinv));
+    k.Mx = f2(cx.M); k.nMx = f2(-cx.M); k.Z1x = f2(cx.Z1); k.Z2x = f2(cx.Z2);
+    k.My = f2(cy.M); k.nMy = f2(-cy.M); k.Z1y = f2(cy.Z1); k.Z2y = f2(cy.Z2);
+    for (int q = 0; q < 4; q++) { k.Fx[q] = f2(cx.F[q]); k.Fy[q] = f2(cy.F[q]); k.Uf[q] = f2(cx.Uf[q]); }
+    return k;
+}
+
+// What a step needs of its tile's frame, as FP32 values, pairs and FP32x2 coefficients (written
+// once per fold window by k_tileconst2d, so that no step does FP64 arithmetic)
 struct TileC2 {
-    AnchorCoef cx, cy;      // split-flux coefficients (x, y)
     float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
     float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
     float dn[4][4][2];      // U*(neighbour) - U*(this) as pairs: [west, east, south, north][comp]
+    Coef2D cf;              // split-flux coefficients, duplicated into both lanes
 };
 constexpr int kTileC2Words = (int)(sizeof(TileC2) / 4);
-constexpr int kTileC2ConstOff = (int)(2 * sizeof(AnchorCoef) / 4);  // first word of wc
 static_assert(sizeof(TileC2) % 4 == 0, "word copy");
 
 __device__ void make_frame2(Frame2& f, const double U[4], const Dom2& d) {
@@ -182,23 +198,6 @@ __device__ __forceinline__ void dflux2(const AnchorCoef& cx, const AnchorCoef& c
     }
 }
 
-
-// anchor coefficients of a 2D tile frame, each duplicated into both FP32x2 lanes
-struct Coef2D {
-    float2 rho, u, v, nu, nv, ne, T, a, gR, R, cvinv, P, m, n, E, gm1;
-    float2 Mx, nMx, Z1x, Z2x, My, nMy, Z1y, Z2y;
-    float2 Fx[4], Fy[4], Uf[4];
-};
-__device__ __forceinline__ Coef2D coef2d(const AnchorCoef& cx, const AnchorCoef& cy) {
-    Coef2D k;
-    k.rho = f2(cx.rho); k.u = f2(cx.u); k.v = f2(cx.v); k.nu = f2(-cx.u); k.nv = f2(-cx.v); k.ne = f2(-cx.e);
-    k.T = f2(cx.T); k.a = f2(cx.a); k.gR = f2(cx.gR); k.R = f2(cx.R); k.cvinv = f2(cx.cvinv); k.P = f2(cx.P);
-    k.m = f2(cx.Uf[1]); k.n = f2(cx.Uf[2]); k.E = f2(cx.Uf[3]); k.gm1 = f2(__fmul_rn(cx.R, cx.cvinv));
-    k.Mx = f2(cx.M); k.nMx = f2(-cx.M); k.Z1x = f2(cx.Z1); k.Z2x = f2(cx.Z2);
-    k.My = f2(cy.M); k.nMy = f2(-cy.M); k.Z1y = f2(cy.Z1); k.Z2y = f2(cy.Z2);
-    for (int q = 0; q < 4; q++) { k.Fx[q] = f2(cx.F[q]); k.Fy[q] = f2(cy.F[q]); k.Uf[q] = f2(cx.Uf[q]); }
-    return k;
-}
 
 // dflux2 for two cells at once (same deviation identities, lane by lane; the minus fluxes from
 // dfp + dfm = dF)
@@ -397,9 +396,7 @@ __global__ void __launch_bounds__(32) k_tileconst2d(Args2 A) {
     const int tb = D.tile_base + tile.ti * D.tiles_j + tile.tj;
     const Frame2& f = A.frames[tb];
     TileC2& c = A.tc[tb];
-    for (int q = tid; q < kTileC2ConstOff; q += 32)
-        reinterpret_cast<float*>(&c)[q] = q < (int)(sizeof(AnchorCoef) / 4)
-            ? reinterpret_cast<const float*>(&f.cx)[q] : reinterpret_cast<const float*>(&f.cy)[q - sizeof(AnchorCoef) / 4];
+    if (tid == 16) c.cf = coef2d(f.cx, f.cy);
     if (tid < 16) {
         // constant wall terms: lam*(W_const - Fref) (west/south), lam*(Fref - W_const) (east/north)
         const int w = tid / 4, k = tid % 4;
@@ -433,13 +430,14 @@ constexpr int WP = TJ / 2 + 2;    // window pairs per row (cells j0-2 .. j0+TJ+1
 
 struct Smem2 {
     float2 f[16][WR][WP];   // dfp0..3, dfm0..3, dhp0..3, dhm0..3 of the window pairs
-    float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
-    float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
-    float dn[4][4][2];      // U*(neighbour) - U*(this) as pairs: [west, east, south, north][comp]
+    float wc[4][4][2];      // the tile's step constants (a copy of its TileC2)
+    float lf[2][4][2];
+    float dn[4][4][2];
+    Coef2D cf;
 };
 
 template <bool KAHAN, bool LAM_POW2>
-__global__ void __launch_bounds__(NTP) k_step2d(Args2 A) {
+__global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
     __shared__ Smem2 S;
     const TileD tile = A.tiles[blockIdx.x];
     const Dom2 D = A.doms[tile.dom];
@@ -455,12 +453,10 @@ __global__ void __launch_bounds__(NTP) k_step2d(Args2 A) {
     float* pho = (kw & 1) ? A.Ph[0] : A.Ph[1];
     float* plo = (kw & 1) ? A.Pl[0] : A.Pl[1];
     const int pp = (A.step - 1) & 1;                     // edge buffers of the previous step
-    // the tile's step constants (one word per thread; read after the barrier below), and its
-    // split-flux coefficients from the table (the same words for every thread)
-    const TileC2& tc = A.tc[tb];
-    if (tid < kTileC2Words - kTileC2ConstOff)
-        reinterpret_cast<float*>(&S.wc)[tid] = reinterpret_cast<const float*>(&tc)[kTileC2ConstOff + tid];
-    const Coef2D c2 = coef2d(tc.cx, tc.cy);
+    // the tile's step constants and coefficients, one word per thread into shared memory (read
+    // from there after the barrier below, which keeps them out of the registers)
+    if (tid < kTileC2Words)
+        reinterpret_cast<float*>(&S.wc)[tid] = reinterpret_cast<const float*>(&A.tc[tb])[tid];
 
     // ---- this thread's window pair ----
     int r, c, nb;   // window row and pair column; owner tile of the cells (-1 this, 0 W, 1 E, 2 S, 3 N)
@@ -477,6 +473,7 @@ __global__ void __launch_bounds__(NTP) k_step2d(Args2 A) {
     }
     const int ci = i0 + r - 1, cj = j0 + 2 * c - 2;     // cell of lane x; lane y is (ci, cj + 1)
     float2 Ph[4], Pl[4];                                 // own increment pairs
+    __syncthreads();
     {
         float2 fp[4], fm[4], hp[4], hm[4];
         float2 d[4];
@@ -500,12 +497,12 @@ __global__ void __launch_bounds__(NTP) k_step2d(Args2 A) {
                     // deviation from this tile's frame: C (relative to the owner's frame) + the
                     // owner's frame offset + the increments
                     float base = A.C[idx];
-                    if (nb >= 0) base = __fadd_rn(__fadd_rn(base, tc.dn[nb][k][0]), tc.dn[nb][k][1]);
+                    if (nb >= 0) base = __fadd_rn(__fadd_rn(base, S.dn[nb][k][0]), S.dn[nb][k][1]);
                     set_lane(d[k], q, __fadd_rn(base, __fadd_rn(h, l)));
                 }
             }
         }
-        dflux2x2(c2, d, fp, fm, hp, hm);
+        dflux2x2(S.cf, d, fp, fm, hp, hm);
         // every slot is written (inactive pairs with the frame's own zero deviations, so that a
         // masked-out neighbour read is finite), except that in a tile cut short in i the east halo
         // row coincides with the first unowned row: there the halo thread writes
