@@ -435,7 +435,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64"
             else args.precision, "data": "synthetic",
             "config": dict(config, cell_updates_per_run=prob.cu, precision=args.precision,
-                           fold_steps=args.fold or ("autotuned" if prob.tuning() else (64 if prob.dim == 1 else 16)),
+                           fold_steps=args.fold or ("autotuned" if prob.tuning() else 64),
                            tuning=prob.tuning(),
                            parallelism=f"replicas{world}",
                            l2="flushed between runs (256 MB write)"),

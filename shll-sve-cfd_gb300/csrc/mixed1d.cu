@@ -44,7 +44,7 @@ constexpr int MW = 512;       // window capacity (cells) of one CTA
 constexpr int MT = MW / 2;    // threads per CTA: two adjacent cells per thread (FP32x2 lanes)
 constexpr int kSweepSteps = 16;      // steps per sweep (temporal blocking depth)
 constexpr int kDefaultFold1D = 64;   // default FP64 fold interval (steps), 1D
-constexpr int kDefaultFold2D = 16;   // 2D
+constexpr int kDefaultFold2D = 64;   // 2D
 
 struct TubeP {
     long base;        // offset of cell 0 in the planes
