@@ -47,8 +47,7 @@ namespace {
 
 constexpr int TI = 16;           // tile rows (x, the slow index)
 constexpr int TJ = 32;           // tile columns (y, contiguous)
-constexpr int NT = TI * TJ;      // threads per CTA, one cell each
-constexpr int WI = TI + 2, WJ = TJ + 2;
+constexpr int NT = TI * TJ;      // threads of the fold kernel, one cell each
 
 struct Dom2 {
     int base;                 // cell offset of the domain in the planes
@@ -130,73 +129,6 @@ __device__ void make_frame2(Frame2& f, const double U[4], const Dom2& d) {
     f.cy.M = (float)My; f.cy.Z1 = (float)Z1y; f.cy.Z2 = (float)Z2y;
 }
 
-// 2D split-flux deviations of a cell with conserved deviation d = (drho, dm, dn, dE):
-// x fluxes (dfp, dfm) with M = u/a and y fluxes (dhp, dhm) with M = v/a (base_shll_2d.c:239-300)
-__device__ __forceinline__ void dflux2(const AnchorCoef& cx, const AnchorCoef& cy, const float d[4], float dfp[4],
-                                       float dfm[4], float dhp[4], float dhm[4]) {
-    const float drho = d[0], dm = d[1], dn = d[2], dE = d[3];
-    const float rho = __fadd_rn(cx.rho, drho);
-    const float r = fast_rcp(rho);
-    const float du = __fmul_rn(__fmaf_rn(-cx.u, drho, dm), r);
-    const float dv = __fmul_rn(__fmaf_rn(-cx.v, drho, dn), r);
-    const float u = __fadd_rn(cx.u, du), v = __fadd_rn(cx.v, dv);
-    const float de = __fmul_rn(__fmaf_rn(-cx.e, drho, dE), r);
-    const float ke = __fmaf_rn(__fadd_rn(u, cx.u), du, __fmul_rn(__fadd_rn(v, cx.v), dv));  // d(u^2+v^2)
-    const float dT = __fmul_rn(__fmaf_rn(-0.5f, ke, de), cx.cvinv);
-    const float T = __fadd_rn(cx.T, dT);
-    const float gRT = __fmul_rn(cx.gR, T);
-    const float ainv = rsqrtf(gRT);
-    const float a = __fmul_rn(gRT, ainv);
-    const float da = __fmul_rn(__fmul_rn(cx.gR, dT), fast_rcp(__fadd_rn(a, cx.a)));
-    const float dP = __fmul_rn(cx.R, __fmaf_rn(drho, T, __fmul_rn(cx.rho, dT)));
-    const float P = __fadd_rn(cx.P, dP);
-    const float E = __fadd_rn(cx.Uf[3], dE);
-    const float EP = __fadd_rn(E, P), dEP = __fadd_rn(dE, dP);
-    // x direction
-    {
-        const float dM = __fmul_rn(__fmaf_rn(-cx.M, da, du), ainv);
-        const float M = __fadd_rn(cx.M, dM);
-        const float dZ1 = __fmul_rn(0.5f, dM);
-        const float Z1 = __fadd_rn(cx.Z1, dZ1), Z3 = __fadd_rn(Z1, -1.0f);
-        const float dZ2 = __fmul_rn(0.5f, __fmaf_rn(da, __fmaf_rn(-M, M, 1.0f), -__fmul_rn(__fmul_rn(cx.a, __fadd_rn(M, cx.M)), dM)));
-        const float Z2 = __fadd_rn(cx.Z2, dZ2);
-        float dF[4];
-        dF[0] = dm;
-        dF[1] = __fadd_rn(__fmaf_rn(dm, u, __fmul_rn(cx.Uf[1], du)), dP);
-        dF[2] = __fmaf_rn(dm, v, __fmul_rn(cx.Uf[1], dv));
-        dF[3] = __fmaf_rn(du, EP, __fmul_rn(cx.u, dEP));
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const float a1 = __fmaf_rn(dF[k], Z1, __fmul_rn(cx.F[k], dZ1));
-            const float a2 = __fmaf_rn(d[k], Z2, __fmul_rn(cx.Uf[k], dZ2));
-            const float a3 = __fmaf_rn(dF[k], Z3, __fmul_rn(cx.F[k], dZ1));
-            dfp[k] = __fadd_rn(a1, a2);
-            dfm[k] = -__fadd_rn(a3, a2);
-        }
-    }
-    // y direction
-    {
-        const float dM = __fmul_rn(__fmaf_rn(-cy.M, da, dv), ainv);
-        const float M = __fadd_rn(cy.M, dM);
-        const float dZ1 = __fmul_rn(0.5f, dM);
-        const float Z1 = __fadd_rn(cy.Z1, dZ1), Z3 = __fadd_rn(Z1, -1.0f);
-        const float dZ2 = __fmul_rn(0.5f, __fmaf_rn(da, __fmaf_rn(-M, M, 1.0f), -__fmul_rn(__fmul_rn(cy.a, __fadd_rn(M, cy.M)), dM)));
-        const float Z2 = __fadd_rn(cy.Z2, dZ2);
-        float dH[4];
-        dH[0] = dn;
-        dH[1] = __fmaf_rn(dn, u, __fmul_rn(cy.Uf[2], du));
-        dH[2] = __fadd_rn(__fmaf_rn(dn, v, __fmul_rn(cy.Uf[2], dv)), dP);
-        dH[3] = __fmaf_rn(dv, EP, __fmul_rn(cy.v, dEP));
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const float a1 = __fmaf_rn(dH[k], Z1, __fmul_rn(cy.F[k], dZ1));
-            const float a2 = __fmaf_rn(d[k], Z2, __fmul_rn(cy.Uf[k], dZ2));
-            const float a3 = __fmaf_rn(dH[k], Z3, __fmul_rn(cy.F[k], dZ1));
-            dhp[k] = __fadd_rn(a1, a2);
-            dhm[k] = -__fadd_rn(a3, a2);
-        }
-    }
-}
 
 
 // dflux2 for two cells at once (same deviation identities, lane by lane; the minus fluxes from
