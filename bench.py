@@ -364,6 +364,22 @@ def reference_arm(args, workload, W):
     return value, ms, sample, cores
 
 
+def max_over_ranks(x, dist, device):
+    """The slowest rank's figure (replicas: the job ends when the last rank ends)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_value(world, cell_updates_per_run, runs, seconds):
+    """Whole-job cell-updates/s: every rank runs its own replica of the workload (weak scaling)."""
+    return world * cell_updates_per_run * runs / seconds
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,13 +453,8 @@ def main():
             launches += shll.kernel_launches() - la
             times.append(e0.elapsed_time(e1) / 1000.0)
     torch.cuda.synchronize()
-    t_total = sum(times)
-    if dist:
-        t = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
-        dist.barrier()
-    value = world * prob.cu * args.steps / t_total
+    t_total = max_over_ranks(sum(times), dist, "cuda")
+    value = job_value(world, prob.cu, args.steps, t_total)
     ms_per_step = 1000 * t_total / args.steps
     mixed_out = prob.result()
 
