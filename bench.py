@@ -225,16 +225,15 @@ class Problem:
             self.obj.checkpoint()
 
     def tuning(self):
-        """The autotuner's choices: {"sweep_steps/fold_steps": items}."""
+        """The autotuner's choices: {"sweep steps/fold steps/chunk cells": items}."""
         if self.dim != 1 or not self.precision.startswith("mixed"):
             return None
         if not self.batch:
-            b, f = self.obj.tuning()
-            return {f"{b}/{f}": 1}
+            return {"%d/%d/%d" % self.obj.tuning(): 1}
         out = {}
         for i in range(len(self.items)):
-            b, f = self.obj.tuning(i)
-            out[f"{b}/{f}"] = out.get(f"{b}/{f}", 0) + 1
+            key = "%d/%d/%d" % self.obj.tuning(i)
+            out[key] = out.get(key, 0) + 1
         return out
 
     def reset_from_host(self):

@@ -181,14 +181,15 @@ void shll_batch_destroy(shll_batch* b);
 /* Autotuner of the mixed-precision 1D engine (no counterpart in the reference): times short runs
  * of the batch (trial_steps steps each; 0 picks a length) for candidate sweep lengths (the
  * temporal-blocking depth: 8, 16, 32 steps, which sets each chunk's owned and halo cells) and fold
- * windows (1 to 8 sweeps), first one choice for all tubes, then per size class (order, limiter,
+ * windows (1 to 8 sweeps) and chunk sizes (the largest window, or half of it: more blocks per SM),
+ * first one choice for all tubes, then per size class (order, limiter,
  * floor(log2 cells)) for the classes holding a tenth of the work or more.  The state is restored
  * afterwards (the batch's or context's device checkpoint is replaced by the current state); the
  * choices are kept process-wide and applied to later batches and contexts whose items leave
  * fold_steps at 0.  shll_batch_tuning reports an item's sweep length and fold
- * interval (steps). */
+ * interval (steps) and its owned cells per chunk (any pointer may be NULL). */
 int shll_batch_autotune(shll_batch* b, int trial_steps);
-int shll_batch_tuning(shll_batch* b, int item, int* sweep_steps, int* fold_steps);
+int shll_batch_tuning(shll_batch* b, int item, int* sweep_steps, int* fold_steps, int* chunk_cells);
 
 /* Device-side checkpoint and restore of a mixed-precision 1D batch (no counterpart in the
  * reference); restore also clears the breakdown flags raised after the checkpoint.
@@ -215,7 +216,7 @@ int shll_tube_run_static(const shll_params* p, double* d_cons, long nsteps, void
 
 /* The autotuner for a single mixed-precision 1D context (see shll_batch_autotune). */
 int shll_autotune(shll_ctx* ctx, int trial_steps);
-int shll_tuning(shll_ctx* ctx, int* sweep_steps, int* fold_steps);
+int shll_tuning(shll_ctx* ctx, int* sweep_steps, int* fold_steps, int* chunk_cells);
 
 /* Replay of captured launch sequences (no counterpart in the reference): a mixed-precision 1D run
  * is captured into a CUDA graph the first time its step counts and buffer parities occur and the

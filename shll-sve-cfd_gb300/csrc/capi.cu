@@ -475,9 +475,9 @@ extern "C" int shll_autotune(shll_ctx* c, int trial_steps) {
     return rc;
 }
 
-extern "C" int shll_tuning(shll_ctx* c, int* sweep_steps, int* fold_steps) {
+extern "C" int shll_tuning(shll_ctx* c, int* sweep_steps, int* fold_steps, int* chunk_cells) {
     if (!c || c->plain || c->p.dim != 1) return SHLL_ERR_ARG;
-    return mixed_tuning(c->mixed, 0, sweep_steps, fold_steps);
+    return mixed_tuning(c->mixed, 0, sweep_steps, fold_steps, chunk_cells);
 }
 
 extern "C" long shll_steps_taken(const shll_ctx* c) { return c ? c->steps_taken : -1; }
@@ -778,9 +778,9 @@ extern "C" int shll_batch_autotune(shll_batch* b, int trial_steps) {
     return mixed_autotune(b->m, trial_steps, b->err, sizeof(b->err));
 }
 
-extern "C" int shll_batch_tuning(shll_batch* b, int item, int* sweep_steps, int* fold_steps) {
+extern "C" int shll_batch_tuning(shll_batch* b, int item, int* sweep_steps, int* fold_steps, int* chunk_cells) {
     if (!b || !b->m || item < 0 || item >= b->count) return SHLL_ERR_ARG;
-    return mixed_tuning(b->m, item, sweep_steps, fold_steps);
+    return mixed_tuning(b->m, item, sweep_steps, fold_steps, chunk_cells);
 }
 
 // device-side checkpoint / restore of a mixed-precision 1D batch (restore also clears the

@@ -33,7 +33,7 @@ long mixed_cell_updates(const MixedState* m);
 int mixed_checkpoint(MixedState* m, bool restore, char* err, size_t errlen);
 int mixed_flags(MixedState* m);
 int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t errlen);
-int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps);
+int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps, int* chunk_cells);
 int mixed_item_flags(MixedState* m, int item);
 
 // FP64 plane sums (reduce.cu)

@@ -1206,18 +1206,26 @@ int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
         *ms = best;
         return r;
     };
-    struct Cand { int B, F; };
+    // owned cells per chunk: the largest window (0) or half of it (smaller chunks, more blocks per
+    // SM: they hide each other's barriers and per-sweep latency at the cost of more halo work)
+    struct Cand { int B, F, half; };
     std::vector<Cand> cands;
     for (int B : {8, 16, 32})
         for (int F : {1, 2, 4, 8})
-            if (B * F <= std::max(trial_steps, 128) && B <= MW / 16) cands.push_back({B, F});
+            for (int half : {0, 1})
+                if (B * F <= std::max(trial_steps, 128) && B <= MW / 16) cands.push_back({B, F, half});
     std::map<TuneKey, std::vector<int>> classes;
     for (int t = 0; t < m->nitems; t++) classes[tune_key(m->tubes[t], m->kahan)].push_back(t);
     auto set_class = [&](const std::vector<int>& ts, Cand c) {
-        for (int t : ts) { m->tubes[t].B = c.B; m->tubes[t].fold_sweeps = c.F; m->tubes[t].owned = 0; }
+        for (int t : ts) {
+            TubeP& tp = m->tubes[t];
+            tp.B = c.B;
+            tp.fold_sweeps = c.F;
+            tp.owned = c.half ? std::max(2 * tp.order * c.B, (MW - 2 * tp.order * c.B) / 2) : 0;
+        }
     };
     // 1) one choice for every class
-    Cand best_all = {m->B, 1};
+    Cand best_all = {m->B, 1, 0};
     float best_ms = 1e30f;
     for (const Cand& c : cands) {
         for (auto& kv : classes) set_class(kv.second, c);
@@ -1235,7 +1243,7 @@ int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
         for (int t : kv.second) w += (double)m->tubes[t].n * m->tubes[t].n;
         if (w < 0.1 * work_total || classes.size() == 1) continue;
         for (const Cand& c : cands) {
-            if (c.B == choice[kv.first].B && c.F == choice[kv.first].F) continue;
+            if (c.B == choice[kv.first].B && c.F == choice[kv.first].F && c.half == choice[kv.first].half) continue;
             set_class(kv.second, c);
             float ms = 0;
             rc = trial(&ms);
@@ -1251,16 +1259,20 @@ int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
     if (rc == SHLL_OK) rc = mixed_checkpoint(m, true, err, len);
     if (rc != SHLL_OK) return rc;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    for (auto& kv : choice) g_tune[kv.first] = {kv.second.B, kv.second.F, 0};
+    for (auto& kv : choice) {
+        const TubeP& tp = m->tubes[classes[kv.first][0]];
+        g_tune[kv.first] = {kv.second.B, kv.second.F, tp.owned};
+    }
     return SHLL_OK;
 }
 
-// sweep length and fold interval (steps) chosen for a tube
-int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps) {
+// sweep length and fold interval (steps) and owned cells per chunk chosen for a tube
+int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps, int* chunk_cells) {
     if (m->dim != 1 || item < 0 || item >= m->nitems) return SHLL_ERR_ARG;
     const TubeP& tp = m->tubes[item];
     if (sweep_steps) *sweep_steps = tp.B;
     if (fold_steps) *fold_steps = tp.B * tp.fold_sweeps;
+    if (chunk_cells) *chunk_cells = chunk_owned(tp);
     return SHLL_OK;
 }
 

@@ -247,9 +247,9 @@ class Context:
         return self._ck(lib().shll_autotune(self.h, trial_steps), "autotune")
 
     def tuning(self):
-        b, f = ctypes.c_int(), ctypes.c_int()
-        self._ck(lib().shll_tuning(self.h, ctypes.byref(b), ctypes.byref(f)), "tuning")
-        return b.value, f.value
+        b, f, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().shll_tuning(self.h, ctypes.byref(b), ctypes.byref(f), ctypes.byref(c)), "tuning")
+        return b.value, f.value, c.value
 
     def checkpoint(self):
         return self._ck(lib().shll_checkpoint(self.h), "checkpoint")
@@ -293,10 +293,10 @@ class Batch:
         return self._ck(lib().shll_batch_autotune(self.h, trial_steps), "batch_autotune")
 
     def tuning(self, i):
-        """(sweep length, fold interval) in steps chosen for item i."""
-        b, f = ctypes.c_int(), ctypes.c_int()
-        self._ck(lib().shll_batch_tuning(self.h, i, ctypes.byref(b), ctypes.byref(f)), "batch_tuning")
-        return b.value, f.value
+        """(sweep length, fold interval) in steps and owned cells per chunk chosen for item i."""
+        b, f, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().shll_batch_tuning(self.h, i, ctypes.byref(b), ctypes.byref(f), ctypes.byref(c)), "batch_tuning")
+        return b.value, f.value, c.value
 
     def checkpoint(self):
         """Device-side copy of the state (mixed-precision 1D batches)."""
