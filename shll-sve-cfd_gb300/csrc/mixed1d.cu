@@ -238,9 +238,12 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         if (side == 0) return ch.idL >= 0 ? boundary_correction(bs, ch.idL, ch.id, k) : 0.0;
         return ch.idR >= 0 ? boundary_correction(bs, ch.id, ch.idR, k) : 0.0;
     };
-    // The frame: computed from the anchor cell at the start of a fold window (one thread, then a
-    // barrier), read from the per-chunk table by the other sweeps of the window
-    const Frame1* frp = wstart ? &fr : &A.frames[ch.id];
+    // The frame: computed from the anchor cell at the start of a fold window (one thread), copied
+    // from the per-chunk table by the other sweeps of the window (one word per thread); either way
+    // it is in shared memory after the barrier below
+    const Frame1* frp = &fr;
+    if (!wstart && tid < kFrameWords)
+        reinterpret_cast<unsigned*>(&fr)[tid] = reinterpret_cast<const unsigned*>(&A.frames[ch.id])[tid];
     // corrections and (inside a window) neighbour-frame offsets as FP32 pairs, once per block
     if (tid < 12 && (tid < 6 || !wstart)) {
         const int side = (tid % 6) / 3, k = tid % 3;
@@ -249,7 +252,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             v = corr_of(side, k);
         } else {
             const int nb = side == 0 ? ch.idL : ch.idR;
-            v = nb >= 0 ? A.frames[nb].U[k] - frp->U[k] : 0.0;
+            v = nb >= 0 ? A.frames[nb].U[k] - A.frames[ch.id].U[k] : 0.0;
         }
         float* o = tid < 6 ? S.corrp[side][k] : S.dnb[side][k];
         d2ff_bits(v, o[0], o[1]);
@@ -325,7 +328,6 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         }
     }
     const Coef2 c2 = coef2(frp->c);
-    const float2 lamh2 = f2(lamh), laml2 = f2(laml);
     const bool hasL = ch.idL >= 0, hasR = ch.idR >= 0;
     // loop-invariant roles of this thread's cells (i = tube cell of window cell w)
     auto edge = [&](int w) { const int i = ws + w; return i <= 0 || i >= n - 1; };
@@ -354,8 +356,11 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         if (w >= L) return false;
         return ORDER == 2 ? (w < L - 1 || i == n - 1) : (i < n - 1 && w < L - 1);
     };
-    const float2 inm = make_float2(in_ok(w0) ? 1.f : 0.f, in_ok(w0 + 1) ? 1.f : 0.f);
-    const float2 outm = make_float2(out_ok(w0) ? 1.f : 0.f, out_ok(w0 + 1) ? 1.f : 0.f);
+    // lam per lane and side, 0 where the interface is not applied (the mask folded into lam)
+    const float2 lin2 = make_float2(in_ok(w0) ? lamh : 0.f, in_ok(w0 + 1) ? lamh : 0.f);
+    const float2 lout2 = make_float2(out_ok(w0) ? lamh : 0.f, out_ok(w0 + 1) ? lamh : 0.f);
+    const float2 llin2 = make_float2(in_ok(w0) ? laml : 0.f, in_ok(w0 + 1) ? laml : 0.f);
+    const float2 llout2 = make_float2(out_ok(w0) ? laml : 0.f, out_ok(w0 + 1) ? laml : 0.f);
     // first-order reflective walls: lane q is cell 0 or n-1 (a few threads)
     bool wallq[2];
 #pragma unroll
@@ -418,19 +423,15 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                 IN = add2(make_float2(Ll, Lo.x), Ro);
                 OUT = add2(Lo, make_float2(Ro.y, Rr));
             }
-            float2 ih = mul2(lamh2, IN), oh = mul2(lamh2, OUT);
+            const float2 ih = mul2(lin2, IN), oh = mul2(lout2, OUT);
             float2 il = f2(0.f), ol = f2(0.f);
             if (!LAM_POW2) {
-                il = add2(fma2(lamh2, IN, neg2(ih)), mul2(laml2, IN));
-                ol = add2(fma2(lamh2, OUT, neg2(oh)), mul2(laml2, OUT));
+                il = add2(fma2(lin2, IN, neg2(ih)), mul2(llin2, IN));
+                ol = add2(fma2(lout2, OUT, neg2(oh)), mul2(llout2, OUT));
             }
-            ih = mul2(ih, inm); oh = mul2(oh, outm);
             two_sum_acc2(dh[k], dl[k], ih);
             two_sum_acc2(dh[k], dl[k], neg2(oh));
-            if (!LAM_POW2) {
-                il = mul2(il, inm); ol = mul2(ol, outm);
-                dl[k] = add2(dl[k], sub2(il, ol));
-            }
+            if (!LAM_POW2) dl[k] = add2(dl[k], sub2(il, ol));
             ihk[k] = ih; ohk[k] = oh; ilk[k] = il; olk[k] = ol;
         }
         if (any_rec) {  // the threads of cells a and b-1 (warp-uniform elsewhere)
