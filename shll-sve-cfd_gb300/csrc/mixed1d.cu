@@ -199,6 +199,21 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     const int nsw = (tp.steps + tp.B - 1) / tp.B;
     const bool wstart = jw == 0;
     const bool wend = jw == F - 1 || A.sweep == nsw - 1;
+    // frames of this window written two or more launches ago may be read before the wait (see
+    // k_sweep1d); L2-only loads, as this SM's L1 may hold the previous window's lines
+    const bool early = !wstart && jw >= 2;
+    unsigned fw = 0;
+    double va = 0.0, vb = 0.0;   // threads 0-5: a correction va - vb; 6-11: a frame offset va - vb
+    if (early) {
+        if (tid < kFrameWords) fw = __ldcg(reinterpret_cast<const unsigned*>(&A.frames[ch.id]) + tid);
+        if (tid >= 6 && tid < 12) {
+            const int side = (tid % 6) / 3, k = tid % 3;
+            const int nb = side == 0 ? ch.idL : ch.idR;
+            if (nb >= 0) { va = __ldcg(&A.frames[nb].U[k]); vb = __ldcg(&A.frames[ch.id].U[k]); }
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // (selects rather than indexing the parameter arrays, which would copy them to local memory)
     const void* hin = inb ? A.hi[1] : A.hi[0];
     const float* lin = inb ? A.lo[1] : A.lo[0];
@@ -242,20 +257,29 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     // from the per-chunk table by the other sweeps of the window (one word per thread); either way
     // it is in shared memory after the barrier below
     const Frame1* frp = &fr;
-    if (!wstart && tid < kFrameWords)
-        reinterpret_cast<unsigned*>(&fr)[tid] = reinterpret_cast<const unsigned*>(&A.frames[ch.id])[tid];
-    // corrections and (inside a window) neighbour-frame offsets as FP32 pairs, once per block
-    if (tid < 12 && (tid < 6 || !wstart)) {
+    // every load of this prologue is issued before any of its values is used: a shared-memory
+    // store of a loaded value stalls the warp until that load returns (in-order issue), which
+    // would serialise the L2 round trips
+    if (!wstart && !early && tid < kFrameWords) fw = reinterpret_cast<const unsigned*>(&A.frames[ch.id])[tid];
+    const bool cthread = tid < 12 && (tid < 6 || !wstart);
+    if (cthread) {
         const int side = (tid % 6) / 3, k = tid % 3;
-        double v;
         if (tid < 6) {
-            v = corr_of(side, k);
-        } else {
+            if (A.sweep > 0) {
+                const BSum* bs = ((A.sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
+                if (side == 0 && ch.idL >= 0) { va = bs[ch.idL].s[1][k]; vb = bs[ch.id].s[0][k]; }
+                if (side == 1 && ch.idR >= 0) { va = bs[ch.id].s[1][k]; vb = bs[ch.idR].s[0][k]; }
+            }
+        } else if (!early) {
             const int nb = side == 0 ? ch.idL : ch.idR;
-            v = nb >= 0 ? A.frames[nb].U[k] - A.frames[ch.id].U[k] : 0.0;
+            if (nb >= 0) { va = A.frames[nb].U[k]; vb = A.frames[ch.id].U[k]; }
         }
+    }
+    if (!wstart && tid < kFrameWords) reinterpret_cast<unsigned*>(&fr)[tid] = fw;
+    if (cthread) {   // as FP32 pairs, once per block
+        const int side = (tid % 6) / 3, k = tid % 3;
         float* o = tid < 6 ? S.corrp[side][k] : S.dnb[side][k];
-        d2ff_bits(v, o[0], o[1]);
+        d2ff_bits(va - vb, o[0], o[1]);
     }
     if (wstart) {
         if (tid == 0) {
@@ -526,18 +550,17 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
 
 // One specialised kernel per scheme variant keeps each kernel's code small (the step loop is
 // latency-bound with few warps per SM, so instruction-fetch bubbles show directly).
-// Consecutive sweeps are chained by programmatic dependent launch: a sweep lets the next one
-// launch at once (griddepcontrol.launch_dependents); the next sweep's blocks become resident
-// beside it, read their descriptors (constant during a run) and wait in griddepcontrol.wait
-// until this grid has completed and its memory is visible (a hardware dependency, no polling).
+// Consecutive sweeps are chained by programmatic dependent launch: once a sweep has passed its
+// own griddepcontrol.wait it lets the next one launch (griddepcontrol.launch_dependents); the next
+// sweep's blocks become resident beside it, read what does not depend on it (descriptors, and
+// frames written two or more launches earlier) and wait in griddepcontrol.wait until this grid
+// has completed and its memory is visible (a hardware dependency, no polling).
 template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
 __global__ void __launch_bounds__(MT, 3) k_sweep1d(SweepArgs A) {
     __shared__ Smem1 S;
     const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM>(A, ch, tp, S);
+    sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM>(A, ch, tp, S);   // waits for the previous sweep inside
 }
 
 // scheme variant of a tube: 0/1 first order (lam a power of two or not), 2/3 second order
