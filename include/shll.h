@@ -224,6 +224,15 @@ int shll_tuning(shll_ctx* ctx, int* sweep_steps, int* fold_steps, int* chunk_cel
  * process-wide). */
 void shll_set_graph_replay(int on);
 
+/* Resident runs (no counterpart in the reference): a mixed-precision 1D run whose chunks fit on
+ * the GPU at once (one block per multiprocessor: a tube of up to about 68000 cells at the default
+ * sweep length) and share one scheme variant is one cooperative launch in which every chunk
+ * waits, with a bounded wait, only for its two neighbours' previous sweep, and keeps its frame
+ * and its cells' FP32 pairs on chip between the sweeps of a fold window.  Results are identical
+ * to the one-launch-per-sweep schedule.  on = 0 selects that schedule for every run (default 1;
+ * process-wide).  A wait that gives up makes the run return SHLL_ERR_TIMEOUT. */
+void shll_set_resident(int on);
+
 /* ---- the reference's own entry points on a process-wide default context ----
  * shll_ref_configure() chooses the problem (else base_shll.c's defaults, N = 256, F64). */
 int shll_ref_configure(const shll_params* p);

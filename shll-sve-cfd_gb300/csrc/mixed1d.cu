@@ -17,9 +17,12 @@
 //     lam*Delta with opposite signs (TwoSum into an FP32 value+compensation pair per cell).
 //   * Neighbouring chunks evaluate their shared boundary interface in different frames, so the
 //     two values differ by rounding.  Each chunk records the flux it applied at both of its
-//     boundaries over the sweep; at the next load the right chunk's first cell receives
-//     lam*sum(F_left chunk - F_right chunk), which makes the left chunk's value the one that
-//     counts: mass, momentum and energy are conserved to the rounding of the FP64 state.
+//     boundaries over the sweep; at the end of the next sweep the right chunk's first cell
+//     receives lam*sum(F_left chunk - F_right chunk) (a fix-up kernel applies the last sweep's
+//     after a run), which makes the left chunk's value the one that counts: mass, momentum and
+//     energy are conserved to the rounding of the FP64 state.  Applied at the end, the correction
+//     is not needed before a sweep's first step, and the copies of a cell in two windows stay
+//     identical (both see the stored value).
 //   * At the end of a sweep the pair is added to the stored state: in FP64
 //     (SHLL_PREC_MIXED_F64) or in FP32-pair arithmetic (SHLL_PREC_MIXED_KAHAN).
 #include <cuda_runtime.h>
@@ -163,13 +166,21 @@ struct Smem1 {
     alignas(16) float sfp[2][3][MW];    // split-flux deviations, double-buffered by step parity
     alignas(16) float sfm[2][3][MW];
     float wall[2][3][2];                // constant wall terms (order 1) for cell 0 / n-1
-    float corrp[2][3][2];               // boundary corrections of cells a and b (previous sweep), FP32 pairs
+    float corrp[3][2];                  // correction owed to cell a by the previous sweep, FP32 pairs
     float dnb[2][3][2];                 // U*(left / right neighbour) - U*(this chunk), FP32 pairs
     float rec[2][MW / 16][3][2];        // per-step terms at the chunk's boundary interfaces
 };
 constexpr int kFrameWords = (int)(sizeof(Frame1) / 4);
 static_assert(sizeof(Frame1) % 4 == 0 && kFrameWords <= MT, "frame copy by one word per thread");
 
+
+// loads of values written by other blocks: from L2 (ld.global.cg) in the resident kernel, where
+// this SM's L1 may still hold lines of an earlier sweep of the same launch
+template <bool CG, class T>
+__device__ __forceinline__ T ldx(const T* p) {
+    if (CG) return __ldcg(p);
+    return *p;
+}
 
 // One sweep of one chunk.  Thread t holds window cells w0 = 2t and w0 + 1 as the two lanes of
 // FP32x2 registers.  Per step: split-flux deviations of both cells (packed) -> shared memory
@@ -179,29 +190,35 @@ static_assert(sizeof(Frame1) % 4 == 0 && kFrameWords <= MT, "frame copy by one w
 // The double buffer makes the second barrier of a store/load/store pattern unnecessary: a
 // thread can only overwrite a buffer after every thread has passed the barrier that follows
 // the last reads of it.
-template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
-__device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp, Smem1& S) {
+// RES: called by the resident kernel (k_tube1d), which keeps the frame and the neighbour-frame
+// offsets in shared memory for a whole fold window.  reuse: the owned cells' deviation pairs are
+// taken from dh/dl (this thread's registers after the previous sweep of the same geometry)
+// instead of memory; keep: the next sweep will do so, so only the cells that the neighbours read
+// as halo are stored.
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, bool RES>
+__device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch, const TubeP& tp, Smem1& S,
+                            float2 (&dh)[3], float2 (&dl)[3], const bool reuse, const bool keep) {
     constexpr int R_ = ORDER;  // stencil reach per step
     Frame1& fr = S.fr;
 
     const int tid = threadIdx.x;
     const int n = tp.n;
-    const int steps = min(tp.B, tp.steps - A.sweep * tp.B);
+    const int steps = min(tp.B, tp.steps - sweep * tp.B);
     if (steps <= 0) return;
     const int H = R_ * steps;
     const int ws = max(0, ch.a - H), we = min(n, ch.b + H), L = we - ws;
     const int pa = ch.a - ws, pb = ch.b - ws;  // first owned / one past the last owned, window coords
-    const int inb = (tp.par + A.sweep) & 1, outb = inb ^ 1;
+    const int inb = (tp.par + sweep) & 1, outb = inb ^ 1;
     // position in the fold window: the first sweep reads the stored state and sets the frame,
     // the last one writes the state back; the sweeps between exchange deviation pairs
     const int F = tp.fold_sweeps;
-    const int jw = A.sweep % F;
+    const int jw = sweep % F;
     const int nsw = (tp.steps + tp.B - 1) / tp.B;
     const bool wstart = jw == 0;
-    const bool wend = jw == F - 1 || A.sweep == nsw - 1;
+    const bool wend = jw == F - 1 || sweep == nsw - 1;
     // frames of this window written two or more launches ago may be read before the wait (see
     // k_sweep1d); L2-only loads, as this SM's L1 may hold the previous window's lines
-    const bool early = !wstart && jw >= 2;
+    const bool early = !RES && !wstart && jw >= 2;
     unsigned fw = 0;
     double va = 0.0, vb = 0.0;   // threads 0-5: a correction va - vb; 6-11: a frame offset va - vb
     if (early) {
@@ -212,8 +229,10 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             if (nb >= 0) { va = __ldcg(&A.frames[nb].U[k]); vb = __ldcg(&A.frames[ch.id].U[k]); }
         }
     }
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (!RES) {
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    }
     // (selects rather than indexing the parameter arrays, which would copy them to local memory)
     const void* hin = inb ? A.hi[1] : A.hi[0];
     const float* lin = inb ? A.lo[1] : A.lo[0];
@@ -240,19 +259,17 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
             const int w = w0 + q;
             if (w < L) {
                 const long idx = k * P + base + ws + w;
-                if (!wstart) { uh[q][k] = dhin[idx]; ul[q][k] = dlin[idx]; }
-                else if (KAHAN) { uh[q][k] = static_cast<const float*>(hin)[idx]; ul[q][k] = lin[idx]; }
-                else uin[q][k] = static_cast<const double*>(hin)[idx];
+                if (!wstart) {
+                    if (reuse && w >= pa && w < pb) { uh[q][k] = lane(dh[k], q); ul[q][k] = lane(dl[k], q); }
+                    else { uh[q][k] = ldx<RES>(dhin + idx); ul[q][k] = ldx<RES>(dlin + idx); }
+                } else if (KAHAN) {
+                    uh[q][k] = ldx<RES>(static_cast<const float*>(hin) + idx);
+                    ul[q][k] = ldx<RES>(lin + idx);
+                } else {
+                    uin[q][k] = ldx<RES>(static_cast<const double*>(hin) + idx);
+                }
             }
         }
-    // correction of the previous sweep owed to cell a (side 0, by the left neighbour) or to cell b
-    // (side 1: the right neighbour's first cell, which lies in this window's halo)
-    auto corr_of = [&](int side, int k) -> double {
-        if (A.sweep == 0) return 0.0;
-        const BSum* bs = ((A.sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
-        if (side == 0) return ch.idL >= 0 ? boundary_correction(bs, ch.idL, ch.id, k) : 0.0;
-        return ch.idR >= 0 ? boundary_correction(bs, ch.id, ch.idR, k) : 0.0;
-    };
     // The frame: computed from the anchor cell at the start of a fold window (one thread), copied
     // from the per-chunk table by the other sweeps of the window (one word per thread); either way
     // it is in shared memory after the barrier below
@@ -260,46 +277,46 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     // every load of this prologue is issued before any of its values is used: a shared-memory
     // store of a loaded value stalls the warp until that load returns (in-order issue), which
     // would serialise the L2 round trips
-    if (!wstart && !early && tid < kFrameWords) fw = reinterpret_cast<const unsigned*>(&A.frames[ch.id])[tid];
-    const bool cthread = tid < 12 && (tid < 6 || !wstart);
+    if (!RES && !wstart && !early && tid < kFrameWords) fw = reinterpret_cast<const unsigned*>(&A.frames[ch.id])[tid];
+    // threads 0-2: the correction owed to cell a by the previous sweep, lam*sum(F_left - F_right)
+    // at the interface a-1/2 (the left neighbour's record minus this chunk's), which the owner of
+    // cell a adds at the end of this sweep; threads 6-11: the neighbour-frame offsets
+    const bool cthread = tid < 3 || (tid >= 6 && tid < 12 && !wstart && (!RES || jw == 1));
     if (cthread) {
         const int side = (tid % 6) / 3, k = tid % 3;
-        if (tid < 6) {
-            if (A.sweep > 0) {
-                const BSum* bs = ((A.sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
-                if (side == 0 && ch.idL >= 0) { va = bs[ch.idL].s[1][k]; vb = bs[ch.id].s[0][k]; }
-                if (side == 1 && ch.idR >= 0) { va = bs[ch.id].s[1][k]; vb = bs[ch.idR].s[0][k]; }
+        if (tid < 3) {
+            if (sweep > 0 && ch.idL >= 0) {
+                const BSum* bs = ((sweep - 1) & 1) ? A.bsum[1] : A.bsum[0];
+                va = ldx<RES>(&bs[ch.idL].s[1][k]);
+                vb = ldx<RES>(&bs[ch.id].s[0][k]);
             }
         } else if (!early) {
             const int nb = side == 0 ? ch.idL : ch.idR;
-            if (nb >= 0) { va = A.frames[nb].U[k]; vb = A.frames[ch.id].U[k]; }
+            if (nb >= 0) { va = ldx<RES>(&A.frames[nb].U[k]); vb = ldx<RES>(&A.frames[ch.id].U[k]); }
         }
     }
-    if (!wstart && tid < kFrameWords) reinterpret_cast<unsigned*>(&fr)[tid] = fw;
+    if (!RES && !wstart && tid < kFrameWords) reinterpret_cast<unsigned*>(&fr)[tid] = fw;
     if (cthread) {   // as FP32 pairs, once per block
         const int side = (tid % 6) / 3, k = tid % 3;
-        float* o = tid < 6 ? S.corrp[side][k] : S.dnb[side][k];
+        float* o = tid < 3 ? S.corrp[k] : S.dnb[side][k];
         d2ff_bits(va - vb, o[0], o[1]);
     }
     if (wstart) {
         if (tid == 0) {
             double U[3];
             float Uanc_h[3], Uanc_l[3];
-            const bool corrected = ch.anc == ch.a || ch.anc == ch.b;
             for (int k = 0; k < 3; k++) {
                 const long idx = k * P + base + ch.anc;
                 if (KAHAN) {
-                    Uanc_h[k] = static_cast<const float*>(hin)[idx];
-                    Uanc_l[k] = lin[idx];
+                    Uanc_h[k] = ldx<RES>(static_cast<const float*>(hin) + idx);
+                    Uanc_l[k] = ldx<RES>(lin + idx);
                     U[k] = f2d_bits(Uanc_h[k]) + f2d_bits(Uanc_l[k]);
                 } else {
-                    U[k] = static_cast<const double*>(hin)[idx];
+                    U[k] = ldx<RES>(static_cast<const double*>(hin) + idx);
                 }
-                if (ch.anc == ch.a) U[k] += corr_of(0, k);
-                if (ch.anc == ch.b) U[k] += corr_of(1, k);
             }
             make_frame(fr, U, tp, ORDER == 1 && (ch.idL < 0 || ch.idR < 0));
-            if (KAHAN && !corrected)  // the stored pair itself, so that the anchor cell's deviation is exactly 0
+            if (KAHAN)  // the stored pair itself, so that the anchor cell's deviation is exactly 0
                 for (int k = 0; k < 3; k++) { fr.Uh[k] = Uanc_h[k]; fr.Ul[k] = Uanc_l[k]; }
         }
     }
@@ -318,7 +335,6 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
     }
 
     // ---- the window as deviations from the frame ----
-    float2 dh[3], dl[3];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
         const int w = w0 + q;
@@ -326,7 +342,6 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
         for (int k = 0; k < 3; k++) {
             float h = 0.f, l = 0.f;
             if (w < L) {
-                const bool corrected = w == pa || w == pb;  // cells owed a boundary correction
                 if (!wstart) {
                     // deviation pair relative to the owner's frame -> relative to this frame
                     h = uh[q][k]; l = ul[q][k];
@@ -334,17 +349,9 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                         const int sd = w < pa ? 0 : 1;
                         ff_add(h, l, S.dnb[sd][k][0], S.dnb[sd][k][1], h, l);
                     }
-                    if (corrected) {
-                        const int sd = w == pa ? 0 : 1;
-                        ff_add(h, l, S.corrp[sd][k][0], S.corrp[sd][k][1], h, l);
-                    }
                 } else {
                     if (KAHAN) ff_sub(uh[q][k], ul[q][k], frp->Uh[k], frp->Ul[k], h, l);
                     else d2ff_bits(uin[q][k] - frp->U[k], h, l);
-                    if (corrected) {
-                        const int sd = w == pa ? 0 : 1;
-                        ff_add(h, l, S.corrp[sd][k][0], S.corrp[sd][k][1], h, l);
-                    }
                 }
             }
             set_lane(dh[k], q, h);
@@ -500,7 +507,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
                 two_sum_acc(h, l, S.rec[side][st][k][0]);
                 l = __fadd_rn(l, S.rec[side][st][k][1]);
             }
-            BSum* bout = ((A.sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
+            BSum* bout = ((sweep & 1) ? A.bsum[1] : A.bsum[0]) + ch.id;
             bout->s[side][k] = steps * lam * frp->F[k] + (f2d_bits(h) + f2d_bits(l));
         }
     }
@@ -521,11 +528,18 @@ __device__ void sweep_chunk(const SweepArgs& A, const Chunk& ch, const TubeP& tp
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const long idx = k * P + base + ws + w;
-            const float h = lane(dh[k], q), l = lane(dl[k], q);
+            float h = lane(dh[k], q), l = lane(dl[k], q);
+            if (w == pa && hasL && sweep > 0) {  // the previous sweep's correction of cell a
+                ff_add(h, l, S.corrp[k][0], S.corrp[k][1], h, l);
+                set_lane(dh[k], q, h);
+                set_lane(dl[k], q, l);
+            }
             finite = finite && isfinite(h) && isfinite(l);
             if (!wend) {
-                dhout[idx] = h;
-                dlout[idx] = l;
+                if (!keep || w < pa + H || w >= pb - H) {  // (keep: only the neighbours' halo cells)
+                    dhout[idx] = h;
+                    dlout[idx] = l;
+                }
                 uf[k] = __fadd_rn(frp->Uh[k], h);
             } else if (KAHAN) {
                 float oh, ol;
@@ -560,7 +574,75 @@ __global__ void __launch_bounds__(MT, 3) k_sweep1d(SweepArgs A) {
     __shared__ Smem1 S;
     const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];
-    sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM>(A, ch, tp, S);   // waits for the previous sweep inside
+    float2 dh[3], dl[3];
+    // (waits for the previous sweep inside)
+    sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, false>(A, A.sweep, ch, tp, S, dh, dl, false, false);
+}
+
+// polls of the neighbours' progress counters before a resident block gives up (under a second,
+// at about half a microsecond per poll; a sweep of a co-resident neighbour takes tens of
+// microseconds)
+constexpr long kSpinLimit = 1L << 20;
+// progress counters one 128-byte line apart: a poll then touches only the counter's own line, so
+// the pollers of one chunk do not delay the release stores of the others
+constexpr int kProgStride = 32;
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The resident form of a run: one block per chunk for all sweeps of the run (a cooperative
+// launch, so every block is resident at once).  A chunk's sweep k needs only the previous sweep
+// of its two neighbours (their halo cells, boundary sums and frames), so instead of one launch
+// per sweep each block waits for its neighbours' progress counters (prog[id] = sweeps completed,
+// published with release semantics after the block's stores).  The frame and the neighbour-frame
+// offsets stay in shared memory for a whole fold window, and the owned cells' deviation pairs stay
+// in registers between the sweeps of a window that have the same geometry; only the cells within
+// the halo width of a chunk edge go through memory.  Write-after-read is covered by the same
+// counters: the buffer that sweep k + 1 writes was read by the neighbours' sweep k, which has
+// completed.  Each wait is bounded: a block that gives up sets SHLL_FLAG_TIMEOUT and returns, and
+// so, bounded again, do the blocks waiting for it.
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
+__global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
+    __shared__ Smem1 S;
+    __shared__ int s_ok;
+    const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
+    const TubeP tp = A.tubes[ch.tube];
+    const int nsw = (tp.steps + tp.B - 1) / tp.B;
+    const int F = tp.fold_sweeps;
+    float2 dh[3], dl[3];
+    for (int sw = 0; sw < nsw; sw++) {
+        if (sw > 0) {
+            if (threadIdx.x == 0) {
+                // both counters polled at once (a chunk without a neighbour on one side reads its
+                // own counter there, which is ahead)
+                const unsigned* pl = prog + (long)(ch.idL >= 0 ? ch.idL : ch.id) * kProgStride;
+                const unsigned* pr = prog + (long)(ch.idR >= 0 ? ch.idR : ch.id) * kProgStride;
+                bool ok = false;
+                for (long it = 0; it < kSpinLimit && !ok; it++) {
+                    const unsigned vl = ld_acquire_gpu(pl), vr = ld_acquire_gpu(pr);
+                    ok = vl >= (unsigned)sw && vr >= (unsigned)sw;
+                    if (!ok) __nanosleep(32);
+                }
+                if (!ok) atomicOr(A.flag, SHLL_FLAG_TIMEOUT);
+                s_ok = ok;
+            }
+            __syncthreads();
+            if (!s_ok) return;
+        }
+        // sweeps of B steps inside a fold window share the geometry of the one before
+        const bool reuse = sw % F != 0 && tp.steps - sw * tp.B >= tp.B;
+        const bool keep = sw + 1 < nsw && (sw + 1) % F != 0 && tp.steps - (sw + 1) * tp.B >= tp.B;
+        sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+        __syncthreads();
+        // (the barrier orders the block's stores before thread 0's release at GPU scope)
+        if (threadIdx.x == 0) st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
+    }
 }
 
 // scheme variant of a tube: 0/1 first order (lam a power of two or not), 2/3 second order
@@ -654,6 +736,57 @@ static cudaError_t launch_sweep(int variant, bool kahan, int grid, cudaStream_t 
     }
 }
 
+// resident form of a run (k_tube1d): a cooperative launch of one block per chunk, each alone on
+// its SM (the same shared-memory padding as single-wave sweeps)
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
+static cudaError_t launch_res(int grid, cudaStream_t s, const SweepArgs& A, unsigned* prog, bool check_only) {
+    static unsigned long long attr_set = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !(attr_set & (1ull << dev))) {
+        cudaError_t e = cudaFuncSetAttribute(k_tube1d<ORDER, KAHAN, LAM_POW2, LIM>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, kSoloSmem);
+        if (e != cudaSuccess) return e;
+        attr_set |= 1ull << dev;
+    }
+    if (check_only) {  // every block must be resident at once
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM>,
+                                                                      MT, kSoloSmem);
+        if (e != cudaSuccess) return e;
+        return (long)per_sm * device_sms() >= grid ? cudaSuccess : cudaErrorCooperativeLaunchTooLarge;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(MT);
+    cfg.dynamicSmemBytes = kSoloSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM>, A, prog);
+}
+
+static cudaError_t launch_resident(int variant, bool kahan, int grid, cudaStream_t s, const SweepArgs& A,
+                                   unsigned* prog, bool check_only) {
+    switch (variant * 2 + (kahan ? 1 : 0)) {
+        case 0: return launch_res<1, false, true, 0>(grid, s, A, prog, check_only);
+        case 1: return launch_res<1, true, true, 0>(grid, s, A, prog, check_only);
+        case 2: return launch_res<1, false, false, 0>(grid, s, A, prog, check_only);
+        case 3: return launch_res<1, true, false, 0>(grid, s, A, prog, check_only);
+        case 4: return launch_res<2, false, true, 0>(grid, s, A, prog, check_only);
+        case 5: return launch_res<2, true, true, 0>(grid, s, A, prog, check_only);
+        case 6: return launch_res<2, false, false, 0>(grid, s, A, prog, check_only);
+        case 7: return launch_res<2, true, false, 0>(grid, s, A, prog, check_only);
+        case 8: return launch_res<2, false, true, 1>(grid, s, A, prog, check_only);
+        case 9: return launch_res<2, true, true, 1>(grid, s, A, prog, check_only);
+        case 10: return launch_res<2, false, false, 1>(grid, s, A, prog, check_only);
+        default: return launch_res<2, true, false, 1>(grid, s, A, prog, check_only);
+    }
+}
+
 // Applies the last sweep's boundary corrections of a run to the first owned cell of every chunk
 // that has a left neighbour (the state buffer that holds the tube after the run).
 template <bool KAHAN>
@@ -703,6 +836,8 @@ struct MixedState {
     float* dh[2] = {nullptr, nullptr};   // deviation pairs between the sweeps of a fold window
     float* dl[2] = {nullptr, nullptr};
     Frame1* frames = nullptr;            // per chunk: frame of the current fold window
+    unsigned* prog = nullptr;            // per chunk: sweeps completed in a resident run
+    size_t prog_n = 0;
     // captured launch sequences of earlier runs, replayed when a run repeats (same step counts and
     // buffer parities)
     struct GraphEntry {
@@ -954,6 +1089,7 @@ void mixed_destroy(MixedState* m) {
         cudaFree(m->dh[b]); cudaFree(m->dl[b]);
     }
     cudaFree(m->frames);
+    cudaFree(m->prog);
     for (auto& g : m->graphs) cudaGraphExecDestroy(g.exec);
     cudaFree(m->d_tubes);
     cudaFree(m->d_chunks);
@@ -1035,9 +1171,10 @@ int mixed_load_all(MixedState* m, char* err, size_t len) {
     return SHLL_OK;
 }
 
-// advances every tube by `steps[t]` steps (one launch per sweep of B steps)
-// issues the launches of one run on m->stream: the sweeps of every variant group, then the fix-up
-static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, long nsweeps, long* launches) {
+// issues the launches of one run on m->stream: the sweeps of every variant group (or, resident,
+// one launch for all sweeps of the run's single variant group), then the fix-up
+static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, long nsweeps, long* launches,
+                             bool resident = false) {
     struct Group { int variant, first; std::vector<int> active; };
     std::vector<Group> groups;
     for (int c = 0; c < (int)order.size(); c++) {
@@ -1063,6 +1200,15 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
     A.item_flags = m->d_item_flags;
     A.sweep = 0;
     long n = 0;
+    if (resident) {
+        A.chunk0 = 0;
+        cudaError_t e = cudaMemsetAsync(m->prog, 0, sizeof(unsigned) * kProgStride * order.size(), m->stream);
+        if (e == cudaSuccess)
+            e = launch_resident(groups[0].variant, m->kahan, (int)order.size(), m->stream, A, m->prog, false);
+        if (e != cudaSuccess) return e;
+        n = 1;
+        nsweeps = 0;
+    }
     for (long k = 0; k < nsweeps; k++) {
         A.sweep = (int)k;
         for (const Group& g : groups) {
@@ -1084,6 +1230,37 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
 
 static std::atomic<int> g_graph_replay{1};
 extern "C" void shll_set_graph_replay(int on) { g_graph_replay = on ? 1 : 0; }
+static std::atomic<int> g_resident{1};
+extern "C" void shll_set_resident(int on) { g_resident = on ? 1 : 0; }
+
+// A run is resident (k_tube1d) when its chunks fit on the GPU at once with one block per SM (the
+// single-wave, latency-bound case: a tube of up to about 68000 cells), share one scheme variant,
+// and each chunk owns at least the halo width, so that every halo cell comes from an adjacent
+// chunk.  Larger runs keep one launch per sweep, which fills the SMs with several blocks each.
+static bool resident_run(MixedState* m, const std::vector<Chunk>& order) {
+    if (!g_resident.load() || order.empty() || (long)order.size() > device_sms()) return false;
+    const int v = tube_variant(m->tubes[order[0].tube]);
+    for (const Chunk& c : order) {
+        const TubeP& tp = m->tubes[c.tube];
+        if (tube_variant(tp) != v || c.b - c.a < tp.order * tp.B) return false;
+    }
+    if (m->prog_n < order.size()) {
+        cudaFree(m->prog);
+        m->prog = nullptr;
+        m->prog_n = 0;
+        if (cudaMalloc(&m->prog, sizeof(unsigned) * kProgStride * order.size()) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        m->prog_n = order.size();
+    }
+    SweepArgs none{};
+    if (launch_resident(v, m->kahan, (int)order.size(), m->stream, none, m->prog, true) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
 
 // advances every tube by `steps[t]` steps (one launch per sweep of B steps).  A run whose step
 // counts and buffer parities occur for the second time is captured into a CUDA graph, which later
@@ -1117,7 +1294,9 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     cudaError_t e = allow_solo_padding();
     if (e != cudaSuccess) { snprintf(err, len, "kernel attribute: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     MixedState::GraphEntry* hit = nullptr;
-    const bool replay = g_graph_replay.load() != 0 && !m->tuning;
+    const bool resident = resident_run(m, order);
+    // (a resident run is one launch: nothing to gain from a graph)
+    const bool replay = g_graph_replay.load() != 0 && !m->tuning && !resident;
     if (replay)
         for (auto& g : m->graphs)
             if (g.steps == steps && g.par == m->par) hit = &g;
@@ -1152,7 +1331,7 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
             }
             if (!done) cudaGetLastError();  // capture not possible here: launch directly
         }
-        if (!done) e = issue_run(m, order, nsweeps, &launches);
+        if (!done) e = issue_run(m, order, nsweeps, &launches, resident);
     }
     if (e != cudaSuccess) { snprintf(err, len, "sweep launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     shll_count_launches(launches);

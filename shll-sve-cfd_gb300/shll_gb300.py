@@ -57,6 +57,7 @@ EXPORTS = [
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
     "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
     "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
+    "shll_set_resident",
 ]
 
 
@@ -150,6 +151,11 @@ def kernel_launches():
 def set_graph_replay(on):
     """Replay captured launch sequences of repeated mixed-precision 1D runs (default on)."""
     lib().shll_set_graph_replay(1 if on else 0)
+
+
+def set_resident(on):
+    """Run single-wave mixed-precision 1D runs as one resident launch (default on)."""
+    lib().shll_set_resident(1 if on else 0)
 
 
 class Context:

@@ -109,17 +109,22 @@ def test_single_tube_breakdown_is_reported(shll, oracle, prec):
 
 def test_repeated_run_replays_identically(shll):
     # The first run's launch sequence is captured into a CUDA graph; a run with the same step
-    # counts and buffer parity replays it and must give the same bits.
-    c = shll.Context(shll.params(1, 2, nx=3000, precision="mixed_f64"))
-    c.init_state()
-    c.checkpoint()
-    c.run()
-    first = c.primitives()
-    n1 = shll.kernel_launches()
-    c.restore()
-    c.run()
-    assert np.array_equal(c.primitives(), first)
-    assert shll.kernel_launches() - n1 > 100   # the replay counts its launches too
+    # counts and buffer parity replays it and must give the same bits.  (One launch per sweep: a
+    # tube this small otherwise runs as one resident launch, with nothing to capture.)
+    shll.set_resident(False)
+    try:
+        c = shll.Context(shll.params(1, 2, nx=3000, precision="mixed_f64"))
+        c.init_state()
+        c.checkpoint()
+        c.run()
+        first = c.primitives()
+        n1 = shll.kernel_launches()
+        c.restore()
+        c.run()
+        assert np.array_equal(c.primitives(), first)
+        assert shll.kernel_launches() - n1 > 100   # the replay counts its launches too
+    finally:
+        shll.set_resident(True)
 
 
 def test_autotune_batch_keeps_results_and_conservation(shll, oracle):

@@ -1,0 +1,105 @@
+"""Resident runs of the mixed 1D engine (one cooperative launch per run, each chunk waiting only
+for its neighbours' previous sweep, frames and owned cells' pairs kept on chip within a fold
+window) against the one-launch-per-sweep schedule: the results must be bit-identical, and the
+launch counts show which schedule ran."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx_run(shll, p, calls, resident):
+    """advances one context by the step counts in calls; returns primitives, totals, launches"""
+    shll.set_resident(resident)
+    try:
+        c = shll.Context(p)
+        c.init_state()
+        n0 = shll.kernel_launches()
+        for k in calls:
+            c.step(k)
+        launches = shll.kernel_launches() - n0
+        out, tot = c.primitives(), c.totals()
+        c.close()
+    finally:
+        shll.set_resident(True)
+    return out, tot, launches
+
+
+def _batch_run(shll, items, resident):
+    shll.set_resident(resident)
+    try:
+        b = shll.Batch(items)
+        n0 = shll.kernel_launches()
+        b.run()
+        launches = shll.kernel_launches() - n0
+        out = [b.primitives(i) for i in range(len(items))]
+        tot = [b.totals(i) for i in range(len(items))]
+        b.close()
+    finally:
+        shll.set_resident(True)
+    return out, tot, launches
+
+
+CASES = [
+    # (order, cells, precision, extra params); fold_steps given, so that no tuned choice applies
+    (2, 65536, "mixed_f64", {"fold_steps": 64}),
+    (2, 65536, "mixed_f64", {"fold_steps": 128}),
+    (2, 20000, "mixed_kahan", {"fold_steps": 64}),
+    (1, 30000, "mixed_f64", {"fold_steps": 64}),
+    (1, 30000, "mixed_kahan", {"fold_steps": 32}),
+    (2, 9000, "mixed_f64", {"fold_steps": 64, "cfl": 0.3, "limiter": 1, "mc_alpha": 1.25}),
+    (1, 5000, "mixed_f64", {"fold_steps": 16, "cfl": 0.3}),
+]
+
+
+@pytest.mark.parametrize("order,n,prec,extra", CASES)
+def test_resident_matches_launch_per_sweep(shll, order, n, prec, extra):
+    p = shll.params(1, order, nx=n, precision=prec, **extra)
+    calls = [16 * 37 + 5]   # a partial last sweep and a fold window cut by the run's end
+    a, ta, la = _ctx_run(shll, p, calls, resident=False)
+    b, tb, lb = _ctx_run(shll, p, calls, resident=True)
+    assert lb == 2 and la > 30   # resident launch + fix-up, against one launch per sweep
+    assert np.array_equal(a, b)
+    assert np.array_equal(ta, tb)
+
+
+def test_resident_run_sequence(shll):
+    p = shll.params(1, 2, nx=40000, precision="mixed_f64", fold_steps=128)
+    calls = [7, 100, 16, 333, 1]
+    a, ta, _ = _ctx_run(shll, p, calls, resident=False)
+    b, tb, lb = _ctx_run(shll, p, calls, resident=True)
+    assert lb == 2 * len(calls)
+    assert np.array_equal(a, b)
+    assert np.array_equal(ta, tb)
+
+
+def test_resident_batch_of_tubes(shll):
+    # several tubes of one variant in one resident launch, of different sizes, initial states and
+    # step counts (their blocks finish at different sweeps)
+    rng = np.random.default_rng(5)
+    items = [shll.params(1, 2, nx=int(n), precision="mixed_f64", n_steps=int(k), fold_steps=64,
+                         ic_rho_l=float(rng.uniform(2, 10)), ic_x_d=float(rng.uniform(0.3, 0.7)))
+             for n, k in ((3000, 700), (11000, 333), (7000, 1000), (20000, 517))]
+    a, ta, la = _batch_run(shll, items, resident=False)
+    b, tb, lb = _batch_run(shll, items, resident=True)
+    assert lb == 2 and la > 30
+    for i in range(len(items)):
+        assert np.array_equal(a[i], b[i]), i
+        assert np.array_equal(ta[i], tb[i])
+
+
+def test_resident_full_sod_run_vs_exact_riemann(shll, oracle):
+    # the whole second-order run of a 16384-cell tube as one launch: mass conserved and the
+    # solution at the exact Riemann solution's distance
+    n = 16384
+    c = shll.Context(shll.params(1, 2, nx=n, precision="mixed_f64", fold_steps=128))
+    c.init_state()
+    t0 = c.totals()
+    n0 = shll.kernel_launches()
+    steps = c.run()
+    assert shll.kernel_launches() - n0 == 2
+    t1 = c.totals()
+    ex = oracle.riemann_exact(n, steps * (0.125 / n))
+    assert np.mean(np.abs(c.primitives()[0] - ex[0])) < 0.003
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+    c.close()
