@@ -460,7 +460,9 @@ def main():
     # roofline of the dominant kernel: algorithmic bytes / (timed region / its launches)
     hbm, peak_kind = peaks()
     bytes_per_cu = 64.0 if prob.dim == 2 else 48.0
-    kernel = "k_step2d" if prob.dim == 2 else "k_sweep1d"
+    # 1D runs that fit on the GPU at once are one resident launch (k_tube1d) plus the fix-up;
+    # larger ones one k_sweep1d launch per sweep
+    kernel = "k_step2d" if prob.dim == 2 else ("k_tube1d" if launches == 2 * args.steps else "k_sweep1d")
     main_launches = max(1, launches - args.steps)  # minus the one fix-up launch per run
     avg_launch = t_total / main_launches
     bytes_per_launch = bytes_per_cu * prob.cu * args.steps / main_launches

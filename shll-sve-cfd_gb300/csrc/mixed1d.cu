@@ -296,7 +296,9 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
         }
     }
     if (!RES && !wstart && tid < kFrameWords) reinterpret_cast<unsigned*>(&fr)[tid] = fw;
-    if (cthread) {   // as FP32 pairs, once per block
+    // as FP32 pairs, once per block; the resident kernel converts the correction only after the
+    // steps, so that its loads do not hold up the first step
+    if (cthread && !(RES && tid < 3)) {
         const int side = (tid % 6) / 3, k = tid % 3;
         float* o = tid < 3 ? S.corrp[k] : S.dnb[side][k];
         d2ff_bits(va - vb, o[0], o[1]);
@@ -320,7 +322,9 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
                 for (int k = 0; k < 3; k++) { fr.Uh[k] = Uanc_h[k]; fr.Ul[k] = Uanc_l[k]; }
         }
     }
-    __syncthreads();
+    // (a resident sweep inside a window after its second writes no shared memory before its first
+    // step: frame and neighbour offsets are kept, the correction is converted later)
+    if (!RES || jw < 2) __syncthreads();
     if (wstart && !wend && tid < kFrameWords)  // keep the frame for the rest of the window
         reinterpret_cast<unsigned*>(&A.frames[ch.id])[tid] = reinterpret_cast<const unsigned*>(&fr)[tid];
     if (tid < 6 && ORDER == 1) {
@@ -497,6 +501,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
             }
         }
     }
+    if (RES && tid < 3) d2ff_bits(va - vb, S.corrp[tid][0], S.corrp[tid][1]);   // (read after the barrier)
     // ---- boundary flux sums of this sweep (full flux: steps * lam * Fref + sum lam*Delta) ----
     __syncthreads();
     if (tid < 6) {
