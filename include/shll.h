@@ -233,6 +233,12 @@ void shll_set_graph_replay(int on);
  * process-wide).  A wait that gives up makes the run return SHLL_ERR_TIMEOUT. */
 void shll_set_resident(int on);
 
+/* Test hook (no counterpart in the reference): in resident runs the chunk with this index (chunks
+ * are numbered along the tubes from 0) never publishes its progress, so its neighbours' bounded
+ * waits run out and the run returns SHLL_ERR_TIMEOUT; -1 (the default) switches it off.
+ * Process-wide. */
+void shll_debug_stall_chunk(int chunk);
+
 /* ---- the reference's own entry points on a process-wide default context ----
  * shll_ref_configure() chooses the problem (else base_shll.c's defaults, N = 256, F64). */
 int shll_ref_configure(const shll_params* p);

@@ -153,6 +153,7 @@ struct SweepArgs {
     int chunk0;         // first chunk of the launch (chunks are grouped by scheme variant)
     int* flag;
     int* item_flags;    // per tube (may be null)
+    int stall_id;       // resident runs, test hook: this chunk never publishes its progress (-1: none)
 };
 
 // correction owed to the first owned cell of the chunk with id `right` by its left neighbour
@@ -632,7 +633,13 @@ __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
                 for (long it = 0; it < kSpinLimit && !ok; it++) {
                     const unsigned vl = ld_acquire_gpu(pl), vr = ld_acquire_gpu(pr);
                     ok = vl >= (unsigned)sw && vr >= (unsigned)sw;
-                    if (!ok) __nanosleep(32);
+                    if (!ok) {
+                        // another block gave up: so does this one (now rather than after its own
+                        // limit; every 64th poll, as all blocks read this word)
+                        if ((it & 63) == 63 && (ld_acquire_gpu(reinterpret_cast<const unsigned*>(A.flag)) & SHLL_FLAG_TIMEOUT))
+                            break;
+                        __nanosleep(32);
+                    }
                 }
                 if (!ok) atomicOr(A.flag, SHLL_FLAG_TIMEOUT);
                 s_ok = ok;
@@ -646,7 +653,7 @@ __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
         sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
         __syncthreads();
         // (the barrier orders the block's stores before thread 0's release at GPU scope)
-        if (threadIdx.x == 0) st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
+        if (threadIdx.x == 0 && ch.id != A.stall_id) st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
     }
 }
 
@@ -1176,6 +1183,13 @@ int mixed_load_all(MixedState* m, char* err, size_t len) {
     return SHLL_OK;
 }
 
+static std::atomic<int> g_graph_replay{1};
+extern "C" void shll_set_graph_replay(int on) { g_graph_replay = on ? 1 : 0; }
+static std::atomic<int> g_resident{1};
+extern "C" void shll_set_resident(int on) { g_resident = on ? 1 : 0; }
+static std::atomic<int> g_stall{-1};
+extern "C" void shll_debug_stall_chunk(int chunk) { g_stall = chunk; }
+
 // issues the launches of one run on m->stream: the sweeps of every variant group (or, resident,
 // one launch for all sweeps of the run's single variant group), then the fix-up
 static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, long nsweeps, long* launches,
@@ -1203,6 +1217,7 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
     A.plane = m->plane;
     A.flag = m->d_flag;
     A.item_flags = m->d_item_flags;
+    A.stall_id = resident ? g_stall.load() : -1;
     A.sweep = 0;
     long n = 0;
     if (resident) {
@@ -1233,10 +1248,6 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
     return cudaGetLastError();
 }
 
-static std::atomic<int> g_graph_replay{1};
-extern "C" void shll_set_graph_replay(int on) { g_graph_replay = on ? 1 : 0; }
-static std::atomic<int> g_resident{1};
-extern "C" void shll_set_resident(int on) { g_resident = on ? 1 : 0; }
 
 // A run is resident (k_tube1d) when its chunks fit on the GPU at once with one block per SM (the
 // single-wave, latency-bound case: a tube of up to about 68000 cells), share one scheme variant,
@@ -1754,6 +1765,7 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.plane = n;
     A.flag = d_flag;
     A.item_flags = nullptr;
+    A.stall_id = -1;
     A.chunk0 = 0;
     const long nsweeps = (nsteps + B - 1) / B;
     shll_count_launches(nsweeps + 1);

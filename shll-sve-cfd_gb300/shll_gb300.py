@@ -57,7 +57,7 @@ EXPORTS = [
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
     "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
     "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
-    "shll_set_resident",
+    "shll_set_resident", "shll_debug_stall_chunk",
 ]
 
 
@@ -156,6 +156,11 @@ def set_graph_replay(on):
 def set_resident(on):
     """Run single-wave mixed-precision 1D runs as one resident launch (default on)."""
     lib().shll_set_resident(1 if on else 0)
+
+
+def debug_stall_chunk(chunk):
+    """Test hook: in resident runs, chunk `chunk` never publishes its progress (-1: off)."""
+    lib().shll_debug_stall_chunk(int(chunk))
 
 
 class Context:

@@ -2,6 +2,8 @@
 for its neighbours' previous sweep, frames and owned cells' pairs kept on chip within a fold
 window) against the one-launch-per-sweep schedule: the results must be bit-identical, and the
 launch counts show which schedule ran."""
+import time
+
 import numpy as np
 import pytest
 
@@ -103,3 +105,24 @@ def test_resident_full_sod_run_vs_exact_riemann(shll, oracle):
     assert np.mean(np.abs(c.primitives()[0] - ex[0])) < 0.003
     assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
     c.close()
+
+
+def test_resident_wait_runs_out_and_is_reported(shll):
+    # a chunk that never publishes its progress (test hook): its neighbours' bounded waits give
+    # up, the other blocks follow as soon as they see the flag, the run reports SHLL_ERR_TIMEOUT
+    # within seconds, and the device stays usable
+    p = shll.params(1, 2, nx=20000, precision="mixed_f64", fold_steps=64)
+    shll.debug_stall_chunk(3)
+    try:
+        c = shll.Context(p)
+        c.init_state()
+        t = time.time()
+        with pytest.raises(shll.ShllError) as e:
+            c.step(16 * 10)
+        assert e.value.status == shll.ERR_TIMEOUT
+        assert time.time() - t < 20
+        c.close()
+    finally:
+        shll.debug_stall_chunk(-1)
+    out, _, launches = _ctx_run(shll, p, [16 * 10], resident=True)
+    assert launches == 2 and np.isfinite(out).all()
