@@ -1,13 +1,15 @@
 // Mixed-precision 1D SHLL engine: FP32 split fluxes in perturbation form, compensated FP32
-// accumulation, FP64 (or FP32-pair) state folded once per sweep.
+// accumulation, FP64 (or FP32-pair) state folded once per fold window of sweeps.
 //
 // Scheme (the arithmetic of base-c/base_shll.c:87-159 and of the x sweep of
 // base-c/2nd_order_base_shll.c:203-459, re-associated as interface fluxes):
 //   * Cells are grouped in chunks (one CTA each).  A chunk is computed over a window of its own
-//     cells plus a halo of order*steps cells on each side (temporal blocking), so one launch
-//     advances every chunk of every tube by a whole sweep of fold_steps steps, with no inter-CTA
-//     waits.
-//   * Every chunk has one frame: the FP64 state U* of an anchor cell at the start of the sweep
+//     cells plus a halo of order*steps cells on each side (temporal blocking), so a sweep
+//     advances every chunk of every tube by B steps with no exchange inside it; a chunk's next
+//     sweep needs only its two neighbours' previous one.  Runs that fit on the GPU at once are one
+//     resident launch in which each chunk waits for its neighbours (k_tube1d); larger ones are
+//     one launch per sweep (k_sweep1d).
+//   * Every chunk has one frame: the FP64 state U* of an anchor cell at the start of the window
 //     (the wall cell for the first and last chunk of a tube, else the centre cell) and the
 //     split-flux coefficients derived from it.  Each window cell's split fluxes are evaluated in
 //     FP32 as deviations from the frame (d fp = fp(U) - fp(U*), d fm likewise), with only
