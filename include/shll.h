@@ -122,7 +122,9 @@ int shll_set_stream(shll_ctx* ctx, void* cuda_stream);
  * from P and P from U (main() :204-205), so the context is ready to step. */
 int shll_init_state(shll_ctx* ctx);
 /* Replaces the primitives (host arrays of nx*ny doubles; v ignored in 1D) and recomputes U and
- * P as shll_init_state does. */
+ * P as shll_init_state does; SHLL_ERR_ARG if a density or temperature is not positive.  In the
+ * mixed modes the arrays are copied as given (at full link speed from pinned host memory) and
+ * converted on the device; shll_get_primitives likewise converts on the device. */
 int shll_set_primitives(shll_ctx* ctx, const double* rho, const double* u, const double* v,
                         const double* T);
 int shll_compute_U_from_P(shll_ctx* ctx);   /* base_shll.c:74-85 */
@@ -171,6 +173,12 @@ int shll_batch_run(shll_batch* b);
 int shll_batch_set_stream(shll_batch* b, void* cuda_stream);
 int shll_batch_get_primitives(shll_batch* b, int item, double* rho, double* u, double* v,
                               double* T);
+/* Replaces item `item`'s state with host primitive planes (v only in 2D), as shll_set_primitives
+ * does for a context: copied as given (at full link speed from pinned host memory) and converted
+ * on the device; SHLL_ERR_ARG with the state unchanged if a density or temperature is not
+ * positive. Mixed-precision batches (SHLL_ERR_UNSUPPORTED for FP64 batches). */
+int shll_batch_set_primitives(shll_batch* b, int item, const double* rho, const double* u,
+                              const double* v, const double* T);
 int shll_batch_totals(shll_batch* b, int item, double* out);
 /* SHLL_OK, or SHLL_ERR_NUMERIC if this item reached a non-positive or NaN density/energy (the
  * other items are unaffected; shll_batch_run returns SHLL_ERR_NUMERIC if any item did). */

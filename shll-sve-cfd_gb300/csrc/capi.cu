@@ -388,6 +388,15 @@ extern "C" int shll_init_state(shll_ctx* c) {
 
 extern "C" int shll_set_primitives(shll_ctx* c, const double* rho, const double* u, const double* v, const double* T) {
     if (!c || !rho || !u || !T || (c->p.dim == 2 && !v)) return SHLL_ERR_ARG;
+    if (!c->plain) {  // copied as given and converted (and checked) on the device
+        const double* planes[4] = {rho, u, c->p.dim == 2 ? v : T, T};
+        c->steps_taken = 0;
+        c->fluxes_valid = false;
+        int rc = mixed_set_item_primitives(c->mixed, 0, planes, c->err, sizeof(c->err));
+        if (rc != SHLL_OK) return rc;
+        c->initialized = true;
+        return check_flag(c);
+    }
     const size_t n = (size_t)c->n;
     std::vector<double> prim(c->nv * n);
     memcpy(prim.data(), rho, n * sizeof(double));
@@ -751,6 +760,21 @@ extern "C" int shll_batch_get_primitives(shll_batch* b, int item, double* rho, d
     if (!b) return SHLL_ERR_ARG;
     if (b->pb) return plain_batch_item_primitives(b->pb, item, rho, u, v, T, b->err, sizeof(b->err));
     return mixed_item_primitives(b->m, item, rho, u, v, T, b->err, sizeof(b->err));
+}
+
+extern "C" int shll_batch_set_primitives(shll_batch* b, int item, const double* rho, const double* u, const double* v,
+                                         const double* T) {
+    if (!b || item < 0 || item >= b->count || !rho || !u || !T) return SHLL_ERR_ARG;
+    if (!b->m) {
+        snprintf(b->err, sizeof(b->err), "host primitives for batch items need a mixed-precision batch");
+        return SHLL_ERR_UNSUPPORTED;
+    }
+    int count = 0;
+    const shll_params* items = mixed_items(b->m, &count);
+    const bool two_d = items[item].dim == 2;
+    if (two_d && !v) return SHLL_ERR_ARG;
+    const double* planes[4] = {rho, u, two_d ? v : T, T};
+    return mixed_set_item_primitives(b->m, item, planes, b->err, sizeof(b->err));
 }
 
 extern "C" int shll_batch_totals(shll_batch* b, int item, double* out) {

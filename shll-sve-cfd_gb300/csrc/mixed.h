@@ -19,6 +19,24 @@ void mixed_set_stream(MixedState* m, cudaStream_t s);
 int mixed_load(MixedState* m, const double* prim, char* err, size_t errlen);
 // loads every item of a batch from its own initial-condition descriptor
 int mixed_load_all(MixedState* m, char* err, size_t errlen);
+// item `item`'s state from host primitive planes (nv pointers: rho, u, [v,] T; pinned host memory
+// is copied at full link speed), converted to conserved variables on the device; SHLL_ERR_ARG,
+// with the state unchanged, if a cell's density or temperature is not positive
+int mixed_set_item_primitives(MixedState* m, int item, const double* const* planes, char* err, size_t errlen);
+
+// where one item's stored state lies (the 1D and 2D engines share the device conversions)
+struct MixedPlanes {
+    void* hi;        // FP64 planes, or the FP32 value planes of a pair state
+    float* lo;       // FP32 compensation planes (pair state) or null
+    long base;       // first cell of the item in every plane
+    long plane;      // cells per plane
+    long n;          // cells of the item
+    int nv;          // conserved components: 3 (1D) or 4 (2D)
+    bool kahan;
+    double CV;       // R / (gamma - 1)
+};
+int mixed2d_planes(MixedState* m, int item, MixedPlanes* out);   // mixed2d.cu
+const shll_params* mixed_items(MixedState* m, int* count);
 // advances every item by nsteps (capped at each item's own remaining steps when nsteps < 0:
 // "run to the end")
 int mixed_step(MixedState* m, long nsteps, char* err, size_t errlen);

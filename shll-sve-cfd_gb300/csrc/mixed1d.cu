@@ -852,6 +852,9 @@ struct MixedState {
     Frame1* frames = nullptr;            // per chunk: frame of the current fold window
     unsigned* prog = nullptr;            // per chunk: sweeps completed in a resident run
     size_t prog_n = 0;
+    double* stage = nullptr;             // device staging of one item's primitive planes
+    size_t stage_words = 0;
+    int* d_bad = nullptr;                // first non-positive cell of an upload
     // captured launch sequences of earlier runs, replayed when a run repeats (same step counts and
     // buffer parities)
     struct GraphEntry {
@@ -1024,7 +1027,6 @@ static TubeP tube_params(const shll_params& p, long base) {
 
 MixedState* mixed2d_attach(MixedState* m, char* err, size_t len);  // mixed2d.cu
 void mixed2d_detach(MixedState* m);
-int mixed2d_load(MixedState* m, int item, const double* prim, char* err, size_t len);
 int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len);
 int mixed2d_item_conserved(MixedState* m, int item, double* planes, char* err, size_t len);
 int mixed2d_totals(MixedState* m, int item, double* out, char* err, size_t len);
@@ -1104,6 +1106,8 @@ void mixed_destroy(MixedState* m) {
     }
     cudaFree(m->frames);
     cudaFree(m->prog);
+    cudaFree(m->stage);
+    cudaFree(m->d_bad);
     for (auto& g : m->graphs) cudaGraphExecDestroy(g.exec);
     cudaFree(m->d_tubes);
     cudaFree(m->d_chunks);
@@ -1125,63 +1129,213 @@ int mixed_flags(MixedState* m) {
     return h;
 }
 
-// writes item t's conserved state (FP64, from primitive planes computed as the FP64 reference
-// does: Compute_U_from_P of base_shll.c:76-80) into buffer par[t]
-static int load_tube(MixedState* m, int t, const double* prim, char* err, size_t len) {
-    const TubeP& tp = m->tubes[t];
-    const int n = tp.n;
-    const double CV = tp.CV;
-    std::vector<double> U(3 * (size_t)n);
-    for (int i = 0; i < n; i++) {
-        double p0 = prim[i], p1 = prim[n + i], p2 = prim[2 * n + i];
-        U[i] = p0;
-        U[n + i] = p0 * p1;
-        U[2 * n + i] = p0 * (p2 * CV + 0.5 * p1 * p1);
+// ---- conversions between primitive planes and the stored state, on the device ----
+// The FP64 arithmetic of Compute_U_from_P (base_shll.c:76-80, base_shll_2d.c:126-136) and of
+// Compute_P_from_U (base_shll.c:171-176, base_shll_2d.c:312-318), in the operation order of a
+// host FP64 evaluation of the same expressions (this unit is compiled without fused multiply-add
+// and uses IEEE division, so the results are the host's bit for bit).
+
+// the lowest cell index whose density or temperature is not positive, stored as n - 1 - i by an
+// atomic maximum (-1: none)
+__global__ void k_check_prim(const double* __restrict__ prim, long n, int nv, int* worst) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double r = prim[i], T = prim[(long)(nv - 1) * n + i];
+        if (!(r > 0.0) || !(T > 0.0)) {
+            atomicMax(worst, (int)(n - 1 - i));
+            break;  // (a thread's later cells have higher indices)
+        }
     }
-    m->par[t] = 0;
-    for (int k = 0; k < 3; k++) {
-        const size_t off = (size_t)k * m->plane + tp.base;
-        if (m->kahan) {
-            std::vector<float> h(n), l(n);
-            for (int i = 0; i < n; i++) {
-                h[i] = (float)U[k * n + i];
-                l[i] = (float)(U[k * n + i] - (double)h[i]);
-            }
-            if (cudaMemcpyAsync(static_cast<float*>(m->hi[0]) + off, h.data(), n * sizeof(float), cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
-                cudaMemcpyAsync(m->lo[0] + off, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
-                cudaStreamSynchronize(m->stream) != cudaSuccess) {
-                snprintf(err, len, "state upload failed");
-                return SHLL_ERR_CUDA;
-            }
+}
+
+template <bool KAHAN>
+__global__ void k_u_from_prim(const double* __restrict__ prim, MixedPlanes s) {
+    const long n = s.n;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double U[4];
+        const double p0 = prim[i], p1 = prim[n + i], p2 = prim[2 * n + i];
+        U[0] = p0;
+        U[1] = p0 * p1;
+        if (s.nv == 3) {
+            U[2] = p0 * (p2 * s.CV + 0.5 * p1 * p1);
         } else {
-            if (cudaMemcpyAsync(static_cast<double*>(m->hi[0]) + off, U.data() + (size_t)k * n, n * sizeof(double),
-                                cudaMemcpyHostToDevice, m->stream) != cudaSuccess) {
-                snprintf(err, len, "state upload failed");
-                return SHLL_ERR_CUDA;
+            const double p3 = prim[3 * n + i];
+            U[2] = p0 * p2;
+            U[3] = p0 * (p3 * s.CV + 0.5 * (p1 * p1 + p2 * p2));
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k >= s.nv) break;
+            const long idx = k * s.plane + s.base + i;
+            if (KAHAN) {
+                const float h = __double2float_rn(U[k]);
+                static_cast<float*>(s.hi)[idx] = h;
+                s.lo[idx] = __double2float_rn(U[k] - (double)h);
+            } else {
+                static_cast<double*>(s.hi)[idx] = U[k];
             }
         }
     }
-    if (cudaStreamSynchronize(m->stream) != cudaSuccess) { snprintf(err, len, "state upload failed"); return SHLL_ERR_CUDA; }
+}
+
+template <bool KAHAN>
+__global__ void k_prim_from_u(MixedPlanes s, double* __restrict__ out) {
+    const long n = s.n;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double U[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k >= s.nv) break;
+            const long idx = k * s.plane + s.base + i;
+            U[k] = KAHAN ? (double)static_cast<const float*>(s.hi)[idx] + (double)s.lo[idx]
+                         : static_cast<const double*>(s.hi)[idx];
+        }
+        const double u0 = U[0], p1 = U[1] / u0;
+        out[i] = u0;
+        out[n + i] = p1;
+        if (s.nv == 3) {
+            out[2 * n + i] = ((U[2] / u0) - 0.5 * p1 * p1) / s.CV;
+        } else {
+            const double p2 = U[2] / u0;
+            out[2 * n + i] = p2;
+            out[3 * n + i] = ((U[3] / u0) - 0.5 * (p1 * p1 + p2 * p2)) / s.CV;
+        }
+    }
+}
+
+static int conv_grid(long n) { return (int)std::max(1L, std::min((n + 255) / 256, (long)device_sms() * 16)); }
+
+// device staging area for nv planes of one item
+static int ensure_stage(MixedState* m, size_t words, char* err, size_t len) {
+    if (m->stage_words >= words && m->d_bad) return SHLL_OK;
+    cudaFree(m->stage);
+    m->stage = nullptr;
+    m->stage_words = 0;
+    if (cudaMalloc(&m->stage, words * sizeof(double)) != cudaSuccess ||
+        (!m->d_bad && cudaMalloc(&m->d_bad, sizeof(int)) != cudaSuccess)) {
+        cudaGetLastError();
+        snprintf(err, len, "cudaMalloc of %zu staging values failed", words);
+        return SHLL_ERR_NOMEM;
+    }
+    m->stage_words = words;
     return SHLL_OK;
+}
+
+// host primitive planes -> stored state of one item (check: refuse non-positive density or
+// temperature first, leaving the state as it was)
+static int upload_prim(MixedState* m, const MixedPlanes& s, const double* const* planes, bool check, char* err,
+                       size_t len) {
+    const size_t n = (size_t)s.n;
+    int rc = ensure_stage(m, (size_t)s.nv * n, err, len);
+    if (rc != SHLL_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < s.nv && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(m->stage + k * n, planes[k], n * sizeof(double), cudaMemcpyHostToDevice, m->stream);
+    if (e == cudaSuccess && check) {
+        int worst = -1;
+        e = cudaMemsetAsync(m->d_bad, 0xff, sizeof(int), m->stream);
+        if (e == cudaSuccess) k_check_prim<<<conv_grid(s.n), 256, 0, m->stream>>>(m->stage, s.n, s.nv, m->d_bad);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&worst, m->d_bad, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        if (e == cudaSuccess && worst >= 0) {
+            snprintf(err, len, "cell %ld: density and temperature must be positive", s.n - 1 - worst);
+            return SHLL_ERR_ARG;
+        }
+    }
+    if (e == cudaSuccess) {
+        if (s.kahan) k_u_from_prim<true><<<conv_grid(s.n), 256, 0, m->stream>>>(m->stage, s);
+        else k_u_from_prim<false><<<conv_grid(s.n), 256, 0, m->stream>>>(m->stage, s);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) { snprintf(err, len, "state upload failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+// stored state of one item -> host primitive planes (null pointers are skipped)
+static int download_prim(MixedState* m, const MixedPlanes& s, double* const* out, char* err, size_t len) {
+    const size_t n = (size_t)s.n;
+    int rc = ensure_stage(m, (size_t)s.nv * n, err, len);
+    if (rc != SHLL_OK) return rc;
+    if (s.kahan) k_prim_from_u<true><<<conv_grid(s.n), 256, 0, m->stream>>>(s, m->stage);
+    else k_prim_from_u<false><<<conv_grid(s.n), 256, 0, m->stream>>>(s, m->stage);
+    cudaError_t e = cudaGetLastError();
+    for (int k = 0; k < s.nv && e == cudaSuccess; k++)
+        if (out[k]) e = cudaMemcpyAsync(out[k], m->stage + k * n, n * sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    if (e != cudaSuccess) { snprintf(err, len, "state download failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+// where item t's state lies (1D: buffer `buf`)
+static MixedPlanes item_planes(MixedState* m, int t, int buf) {
+    MixedPlanes s;
+    if (m->dim == 2) {
+        mixed2d_planes(m, t, &s);
+        return s;
+    }
+    const TubeP& tp = m->tubes[t];
+    s.hi = m->hi[buf];
+    s.lo = m->lo[buf];
+    s.base = tp.base;
+    s.plane = m->plane;
+    s.n = tp.n;
+    s.nv = 3;
+    s.kahan = m->kahan;
+    s.CV = tp.CV;
+    return s;
+}
+
+// one item's state from primitive planes (1D tubes start in buffer 0)
+static int load_item(MixedState* m, int t, const double* const* planes, bool check, char* err, size_t len) {
+    int rc = upload_prim(m, item_planes(m, t, 0), planes, check, err, len);
+    if (rc == SHLL_OK && m->dim == 1) m->par[t] = 0;
+    return rc;
+}
+
+static void plane_ptrs(const double* prim, long n, int nv, const double* out[4]) {
+    for (int k = 0; k < 4; k++) out[k] = k < nv ? prim + k * n : nullptr;
 }
 
 int mixed_load(MixedState* m, const double* prim, char* err, size_t len) {
     cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
     cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
-    if (m->dim == 2) return mixed2d_load(m, 0, prim, err, len);
-    return load_tube(m, 0, prim, err, len);
+    const MixedPlanes s = item_planes(m, 0, 0);
+    const double* planes[4];
+    plane_ptrs(prim, s.n, s.nv, planes);
+    int rc = load_item(m, 0, planes, false, err, len);
+    if (rc == SHLL_OK && cudaStreamSynchronize(m->stream) != cudaSuccess) {
+        snprintf(err, len, "state upload failed");
+        return SHLL_ERR_CUDA;
+    }
+    return rc;
 }
 
 int mixed_load_all(MixedState* m, char* err, size_t len) {
     cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
     cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
+    std::vector<double> prim;
     for (int t = 0; t < m->nitems; t++) {
         const shll_params& p = m->items[t];
-        std::vector<double> prim((size_t)(p.dim == 2 ? 4 : 3) * p.nx * (p.dim == 2 ? p.ny : 1));
+        const int nv = p.dim == 2 ? 4 : 3;
+        const long n = (long)p.nx * (p.dim == 2 ? p.ny : 1);
+        prim.resize((size_t)nv * n);
         shll_ic_fill(&p, 64, prim.data());
-        int rc = m->dim == 2 ? mixed2d_load(m, t, prim.data(), err, len) : load_tube(m, t, prim.data(), err, len);
+        const double* planes[4];
+        plane_ptrs(prim.data(), n, nv, planes);
+        // (a pageable source is copied before the call returns, so the vector can be refilled)
+        int rc = load_item(m, t, planes, false, err, len);
         if (rc != SHLL_OK) return rc;
     }
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) { snprintf(err, len, "state upload failed"); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+int mixed_set_item_primitives(MixedState* m, int item, const double* const* planes, char* err, size_t len) {
+    if (item < 0 || item >= m->nitems) { snprintf(err, len, "item %d out of range", item); return SHLL_ERR_ARG; }
+    int rc = load_item(m, item, planes, true, err, len);
+    if (rc != SHLL_OK) return rc;
+    cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+    cudaMemsetAsync(m->d_item_flags + item, 0, sizeof(int), m->stream);
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) { snprintf(err, len, "state upload failed"); return SHLL_ERR_CUDA; }
     return SHLL_OK;
 }
 
@@ -1537,30 +1691,10 @@ int mixed_item_conserved(MixedState* m, int item, double* planes, char* err, siz
 
 int mixed_item_primitives(MixedState* m, int item, double* rho, double* u, double* v, double* T, char* err, size_t len) {
     if (item < 0 || item >= m->nitems) { snprintf(err, len, "item %d out of range", item); return SHLL_ERR_ARG; }
-    const shll_params& p = m->items[item];
-    const size_t n = (size_t)p.nx * (p.dim == 2 ? p.ny : 1);
-    const int nv = p.dim == 2 ? 4 : 3;
-    std::vector<double> U(nv * n);
-    int rc = mixed_item_conserved(m, item, U.data(), err, len);
-    if (rc != SHLL_OK) return rc;
-    const double CV = p.R / (p.gamma - 1.0);
-    // Compute_P_from_U in FP64 (base_shll.c:171-176 / base_shll_2d.c:312-318)
-    for (size_t c = 0; c < n; c++) {
-        double u0 = U[c];
-        double p1 = U[n + c] / u0;
-        if (nv == 3) {
-            if (rho) rho[c] = u0;
-            if (u) u[c] = p1;
-            if (T) T[c] = ((U[2 * n + c] / u0) - 0.5 * p1 * p1) / CV;
-        } else {
-            double p2 = U[2 * n + c] / u0;
-            if (rho) rho[c] = u0;
-            if (u) u[c] = p1;
-            if (v) v[c] = p2;
-            if (T) T[c] = ((U[3 * n + c] / u0) - 0.5 * (p1 * p1 + p2 * p2)) / CV;
-        }
-    }
-    return SHLL_OK;
+    const MixedPlanes s = item_planes(m, item, m->dim == 1 ? m->par[item] : 0);
+    double* const out3[3] = {rho, u, T};
+    double* const out4[4] = {rho, u, v, T};
+    return download_prim(m, s, s.nv == 3 ? out3 : out4, err, len);
 }
 
 int mixed_get_primitives(MixedState* m, double* rho, double* u, double* v, double* T, char* err, size_t len) {

@@ -664,38 +664,17 @@ void mixed2d_detach(MixedState* m) {
 }
 
 // item's conserved state from primitive planes, U from P in FP64 (base_shll_2d.c:126-131)
-int mixed2d_load(MixedState* m, int item, const double* prim, char* err, size_t len) {
+int mixed2d_planes(MixedState* m, int item, MixedPlanes* out) {
     Mixed2D* d = get2(m);
     const Dom2& D = d->doms[item];
-    const size_t n = (size_t)D.nx * D.ny;
-    std::vector<double> U(4 * n);
-    for (size_t c = 0; c < n; c++) {
-        const double p0 = prim[c], p1 = prim[n + c], p2 = prim[2 * n + c], p3 = prim[3 * n + c];
-        U[c] = p0;
-        U[n + c] = p0 * p1;
-        U[2 * n + c] = p0 * p2;
-        U[3 * n + c] = p0 * (p3 * D.CV + 0.5 * (p1 * p1 + p2 * p2));
-    }
-    cudaStream_t s = mixed_stream(m);
-    for (int k = 0; k < 4; k++) {
-        const size_t off = (size_t)k * d->plane + D.base;
-        cudaError_t e;
-        if (mixed_is_kahan(m)) {
-            std::vector<float> h(n), l(n);
-            for (size_t c = 0; c < n; c++) {
-                h[c] = (float)U[k * n + c];
-                l[c] = (float)(U[k * n + c] - (double)h[c]);
-            }
-            e = cudaMemcpyAsync(static_cast<float*>(d->B) + off, h.data(), n * sizeof(float), cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(d->Blo + off, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        } else {
-            e = cudaMemcpyAsync(static_cast<double*>(d->B) + off, U.data() + k * n, n * sizeof(double),
-                                cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        }
-        if (e != cudaSuccess) { snprintf(err, len, "2D state upload failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
-    }
+    out->hi = d->B;
+    out->lo = d->Blo;
+    out->base = D.base;
+    out->plane = d->plane;
+    out->n = (long)D.nx * D.ny;
+    out->nv = 4;
+    out->kahan = mixed_is_kahan(m);
+    out->CV = D.CV;
     return SHLL_OK;
 }
 

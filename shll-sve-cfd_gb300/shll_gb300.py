@@ -57,7 +57,7 @@ EXPORTS = [
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
     "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
     "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
-    "shll_set_resident", "shll_debug_stall_chunk",
+    "shll_set_resident", "shll_debug_stall_chunk", "shll_batch_set_primitives",
 ]
 
 
@@ -101,6 +101,7 @@ def lib():
         L.shll_batch_set_stream.argtypes = [vp, vp]
         L.shll_batch_item_status.argtypes = [vp, ctypes.c_int]
         L.shll_batch_get_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
+        L.shll_batch_set_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
         L.shll_batch_totals.argtypes = [vp, ctypes.c_int, dp]
         L.shll_batch_cell_updates.argtypes = [vp]
         L.shll_batch_cell_updates.restype = ctypes.c_long
@@ -224,9 +225,12 @@ class Context:
     def steps_taken(self):
         return lib().shll_steps_taken(self.h)
 
-    def primitives(self):
-        """(nv, n) array: rho, u, [v,] T."""
-        out = np.zeros((self.nv, self.n))
+    def primitives(self, out=None):
+        """(nv, n) array: rho, u, [v,] T (into `out`, a C-contiguous float64 array of that shape,
+        for instance a view of pinned host memory, when given)."""
+        if out is None:
+            out = np.zeros((self.nv, self.n))
+        assert out.shape == (self.nv, self.n) and out.dtype == np.float64 and out.flags.c_contiguous
         if self.nv == 3:
             self._ck(lib().shll_get_primitives(self.h, _dp(out[0]), _dp(out[1]), None, _dp(out[2])), "primitives")
         else:
@@ -323,11 +327,21 @@ class Batch:
     def set_stream(self, stream_ptr):
         self._ck(lib().shll_batch_set_stream(self.h, stream_ptr), "batch_set_stream")
 
-    def primitives(self, i):
+    def set_primitives(self, i, rho, u, T, v=None):
+        """Replaces item i's state (host arrays, copied as given and converted on the device)."""
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (rho, u, T)]
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        return self._ck(lib().shll_batch_set_primitives(self.h, i, _dp(arrs[0]), _dp(arrs[1]), _dp(vv), _dp(arrs[2])),
+                        "batch_set_primitives")
+
+    def primitives(self, i, out=None):
+        """(nv, n) array of item i: rho, u, [v,] T (into `out` when given, as Context.primitives)."""
         p = self.items[i]
         n = p.nx * (p.ny if p.dim == 2 else 1)
         nv = 4 if p.dim == 2 else 3
-        out = np.zeros((nv, n))
+        if out is None:
+            out = np.zeros((nv, n))
+        assert out.shape == (nv, n) and out.dtype == np.float64 and out.flags.c_contiguous
         if nv == 3:
             self._ck(lib().shll_batch_get_primitives(self.h, i, _dp(out[0]), _dp(out[1]), None, _dp(out[2])), "prims")
         else:
