@@ -236,18 +236,38 @@ class Problem:
             out[key] = out.get(key, 0) + 1
         return out
 
-    def reset_from_host(self):
-        """Rebuilds the problem from host data (the end-to-end leg: descriptors and initial state
-        uploaded every time)."""
-        if self.obj is not None:
-            self.obj.close()
-            self.obj = None
+    def host_buffers(self, torch):
+        """Pinned host memory for the end-to-end leg: every item's initial primitives (its
+        descriptor's, as the library loads them) and room for its results."""
+        plist = self.items if self.batch else [self.p]
+        shapes = [(4 if p.dim == 2 else 3, p.nx * (p.ny if p.dim == 2 else 1)) for p in plist]
+        total = sum(nv * n for nv, n in shapes)
+        pin_in = torch.empty(total, dtype=torch.float64, pin_memory=True).numpy()
+        pin_out = torch.empty(total, dtype=torch.float64, pin_memory=True).numpy()
+        ins, outs, off = [], [], 0
+        for p, (nv, n) in zip(plist, shapes):
+            ins.append(pin_in[off:off + nv * n].reshape(nv, n))
+            outs.append(pin_out[off:off + nv * n].reshape(nv, n))
+            self.shll.initial_primitives(p, out=ins[-1])
+            off += nv * n
+        self.pin_in, self.pin_out = pin_in, pin_out   # (batches: the packed layout, item after item)
+        return ins, outs
+
+    def upload(self, ins):
+        """The initial state from host memory through the public API (copied as given, converted on
+        the device)."""
+        if self.batch:   # one packed upload for every item
+            self.obj.set_all_primitives(self.pin_in)
+            return
+        b = ins[0]
+        args, kw = ((b[0], b[1], b[2]), {}) if self.dim == 1 else ((b[0], b[1], b[3]), {"v": b[2]})
+        self.obj.set_primitives(*args, **kw)
+
+    def download(self, outs):
         if self.batch:
-            self.obj = self.shll.Batch(self.items)
+            self.obj.get_all_primitives(self.pin_out)
         else:
-            self.obj = self.shll.Context(self.p)
-            self.obj.init_state()
-        self.obj.set_stream(self.stream.cuda_stream)
+            self.obj.primitives(out=outs[0])
 
     def run(self):
         if self.batch:
@@ -473,20 +493,22 @@ def main():
                 "note": "launch duration = CUDA-event time of the timed runs / launches (includes gaps)"}
 
     # end to end through the C-ABI with host buffers: upload the initial state, run, download
+    # (every step: the initial primitives of every item from pinned host memory through
+    # set_primitives, the run, the result primitives back into pinned host memory)
+    host_in, host_out = prob.host_buffers(torch)
     e_times = []
-    h2d = d2h = 0
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        prob.reset_from_host()
+        prob.upload(host_in)
         prob.run()
-        out = prob.result()
+        prob.download(host_out)
         torch.cuda.synchronize()
         e_times.append(time.perf_counter() - t0)
-    nv = 4 if prob.dim == 2 else 3
-    plist = prob.items if prob.batch else [prob.p]
-    cells_total = sum(p.nx * (p.ny if p.dim == 2 else 1) for p in plist)
-    h2d = d2h = nv * 8 * cells_total  # primitives up (or descriptors expanded on the host), primitives down
+    # the end-to-end result is the device-timed run's, bit for bit
+    e2e_identical = all(np.array_equal(a, b, equal_nan=True)
+                        for a, b in zip(host_out, mixed_out if prob.batch else [mixed_out]))
+    h2d = d2h = sum(b.nbytes for b in host_in)
     e2e_value = world * prob.cu * len(e_times) / sum(e_times)
 
     extras = {}
@@ -505,7 +527,8 @@ def main():
                            l2="flushed between runs (256 MB write)"),
             "roofline": roofline,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "host_memory": "pinned",
+                    "result_identical_to_device_run": e2e_identical},
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }

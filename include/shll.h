@@ -121,6 +121,10 @@ int shll_set_stream(shll_ctx* ctx, void* cuda_stream);
 /* Allocate_and_Init_Memory (:28-61): primitives from p->ic on the device.  Also computes U
  * from P and P from U (main() :204-205), so the context is ready to step. */
 int shll_init_state(shll_ctx* ctx);
+/* The initial primitives of p's initial-condition descriptor (host arrays of nx*ny doubles; v
+ * ignored in 1D): the values shll_init_state loads (no counterpart in the reference, whose
+ * Allocate_and_Init_Memory writes them into its globals). */
+int shll_initial_primitives(const shll_params* p, double* rho, double* u, double* v, double* T);
 /* Replaces the primitives (host arrays of nx*ny doubles; v ignored in 1D) and recomputes U and
  * P as shll_init_state does; SHLL_ERR_ARG if a density or temperature is not positive.  In the
  * mixed modes the arrays are copied as given (at full link speed from pinned host memory) and
@@ -179,6 +183,12 @@ int shll_batch_get_primitives(shll_batch* b, int item, double* rho, double* u, d
  * positive. Mixed-precision batches (SHLL_ERR_UNSUPPORTED for FP64 batches). */
 int shll_batch_set_primitives(shll_batch* b, int item, const double* rho, const double* u,
                               const double* v, const double* T);
+/* Every item at once (mixed-precision batches): `prim` holds, item after item in batch order,
+ * each item's planes rho, u, [v,] T of nx*ny doubles.  One host<->device copy each way and one
+ * synchronisation; set checks every item before changing any state (SHLL_ERR_ARG names the first
+ * item and cell with a non-positive density or temperature). */
+int shll_batch_set_all_primitives(shll_batch* b, const double* prim);
+int shll_batch_get_all_primitives(shll_batch* b, double* prim);
 int shll_batch_totals(shll_batch* b, int item, double* out);
 /* SHLL_OK, or SHLL_ERR_NUMERIC if this item reached a non-positive or NaN density/energy (the
  * other items are unaffected; shll_batch_run returns SHLL_ERR_NUMERIC if any item did). */

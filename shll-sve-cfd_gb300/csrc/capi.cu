@@ -386,6 +386,19 @@ extern "C" int shll_init_state(shll_ctx* c) {
     return load_primitives(c, prim.data());
 }
 
+extern "C" int shll_initial_primitives(const shll_params* p, double* rho, double* u, double* v, double* T) {
+    char e[256];
+    if (!p || !rho || !u || !T || (p->dim == 2 && !v)) return SHLL_ERR_ARG;
+    if (validate(p, e, sizeof(e)) != SHLL_OK || p->ic.kind == SHLL_IC_USER) return SHLL_ERR_ARG;
+    const size_t n = (size_t)p->nx * (p->dim == 2 ? p->ny : 1);
+    const int nv = p->dim == 2 ? 4 : 3;
+    std::vector<double> prim((size_t)nv * n);
+    shll_ic_fill(p, p->precision == SHLL_PREC_F32_EXACT ? 32 : 64, prim.data());  // as shll_init_state
+    double* out[4] = {rho, u, p->dim == 2 ? v : T, T};
+    for (int k = 0; k < nv; k++) memcpy(out[k], prim.data() + (size_t)k * n, n * sizeof(double));
+    return SHLL_OK;
+}
+
 extern "C" int shll_set_primitives(shll_ctx* c, const double* rho, const double* u, const double* v, const double* T) {
     if (!c || !rho || !u || !T || (c->p.dim == 2 && !v)) return SHLL_ERR_ARG;
     if (!c->plain) {  // copied as given and converted (and checked) on the device
@@ -775,6 +788,24 @@ extern "C" int shll_batch_set_primitives(shll_batch* b, int item, const double* 
     if (two_d && !v) return SHLL_ERR_ARG;
     const double* planes[4] = {rho, u, two_d ? v : T, T};
     return mixed_set_item_primitives(b->m, item, planes, b->err, sizeof(b->err));
+}
+
+extern "C" int shll_batch_set_all_primitives(shll_batch* b, const double* prim) {
+    if (!b || !prim) return SHLL_ERR_ARG;
+    if (!b->m) {
+        snprintf(b->err, sizeof(b->err), "host primitives for batch items need a mixed-precision batch");
+        return SHLL_ERR_UNSUPPORTED;
+    }
+    return mixed_set_all_primitives(b->m, prim, b->err, sizeof(b->err));
+}
+
+extern "C" int shll_batch_get_all_primitives(shll_batch* b, double* prim) {
+    if (!b || !prim) return SHLL_ERR_ARG;
+    if (!b->m) {
+        snprintf(b->err, sizeof(b->err), "packed primitives need a mixed-precision batch");
+        return SHLL_ERR_UNSUPPORTED;
+    }
+    return mixed_get_all_primitives(b->m, prim, b->err, sizeof(b->err));
 }
 
 extern "C" int shll_batch_totals(shll_batch* b, int item, double* out) {

@@ -23,6 +23,10 @@ int mixed_load_all(MixedState* m, char* err, size_t errlen);
 // is copied at full link speed), converted to conserved variables on the device; SHLL_ERR_ARG,
 // with the state unchanged, if a cell's density or temperature is not positive
 int mixed_set_item_primitives(MixedState* m, int item, const double* const* planes, char* err, size_t errlen);
+// every item at once: `prim` holds, item after item, each item's planes rho, u, [v,] T (one copy
+// each way, one conversion kernel per item, one synchronisation)
+int mixed_set_all_primitives(MixedState* m, const double* prim, char* err, size_t errlen);
+int mixed_get_all_primitives(MixedState* m, double* prim, char* err, size_t errlen);
 
 // where one item's stored state lies (the 1D and 2D engines share the device conversions)
 struct MixedPlanes {

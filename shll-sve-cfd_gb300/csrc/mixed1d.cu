@@ -855,6 +855,7 @@ struct MixedState {
     double* stage = nullptr;             // device staging of one item's primitive planes
     size_t stage_words = 0;
     int* d_bad = nullptr;                // first non-positive cell of an upload
+    int* d_bad_items = nullptr;          // the same per item (uploads of every item at once)
     // captured launch sequences of earlier runs, replayed when a run repeats (same step counts and
     // buffer parities)
     struct GraphEntry {
@@ -1108,6 +1109,7 @@ void mixed_destroy(MixedState* m) {
     cudaFree(m->prog);
     cudaFree(m->stage);
     cudaFree(m->d_bad);
+    cudaFree(m->d_bad_items);
     for (auto& g : m->graphs) cudaGraphExecDestroy(g.exec);
     cudaFree(m->d_tubes);
     cudaFree(m->d_chunks);
@@ -1326,6 +1328,71 @@ int mixed_load_all(MixedState* m, char* err, size_t len) {
         if (rc != SHLL_OK) return rc;
     }
     if (cudaStreamSynchronize(m->stream) != cudaSuccess) { snprintf(err, len, "state upload failed"); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+// every item at once: `prim` holds, item after item, each item's nv planes of n doubles
+static std::vector<long> packed_offsets(MixedState* m) {
+    std::vector<long> off(m->nitems + 1, 0);
+    for (int t = 0; t < m->nitems; t++) {
+        const MixedPlanes s = item_planes(m, t, 0);
+        off[t + 1] = off[t] + (long)s.nv * s.n;
+    }
+    return off;
+}
+
+int mixed_set_all_primitives(MixedState* m, const double* prim, char* err, size_t len) {
+    const std::vector<long> off = packed_offsets(m);
+    int rc = ensure_stage(m, (size_t)off[m->nitems], err, len);
+    if (rc != SHLL_OK) return rc;
+    if (!m->d_bad_items && cudaMalloc(&m->d_bad_items, sizeof(int) * m->nitems) != cudaSuccess) {
+        cudaGetLastError();
+        snprintf(err, len, "cudaMalloc of the check flags failed");
+        return SHLL_ERR_NOMEM;
+    }
+    cudaError_t e = cudaMemcpyAsync(m->stage, prim, sizeof(double) * off[m->nitems], cudaMemcpyHostToDevice, m->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->d_bad_items, 0xff, sizeof(int) * m->nitems, m->stream);
+    for (int t = 0; t < m->nitems && e == cudaSuccess; t++) {
+        const MixedPlanes s = item_planes(m, t, 0);
+        k_check_prim<<<conv_grid(s.n), 256, 0, m->stream>>>(m->stage + off[t], s.n, s.nv, m->d_bad_items + t);
+    }
+    std::vector<int> worst(m->nitems, -1);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(worst.data(), m->d_bad_items, sizeof(int) * m->nitems, cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    if (e != cudaSuccess) { snprintf(err, len, "state upload failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    for (int t = 0; t < m->nitems; t++)
+        if (worst[t] >= 0) {
+            snprintf(err, len, "item %d, cell %ld: density and temperature must be positive", t,
+                     item_planes(m, t, 0).n - 1 - worst[t]);
+            return SHLL_ERR_ARG;
+        }
+    for (int t = 0; t < m->nitems; t++) {
+        const MixedPlanes s = item_planes(m, t, 0);
+        if (s.kahan) k_u_from_prim<true><<<conv_grid(s.n), 256, 0, m->stream>>>(m->stage + off[t], s);
+        else k_u_from_prim<false><<<conv_grid(s.n), 256, 0, m->stream>>>(m->stage + off[t], s);
+        if (m->dim == 1) m->par[t] = 0;
+    }
+    cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+    cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    if (e != cudaSuccess) { snprintf(err, len, "state upload failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+int mixed_get_all_primitives(MixedState* m, double* prim, char* err, size_t len) {
+    const std::vector<long> off = packed_offsets(m);
+    int rc = ensure_stage(m, (size_t)off[m->nitems], err, len);
+    if (rc != SHLL_OK) return rc;
+    for (int t = 0; t < m->nitems; t++) {
+        const MixedPlanes s = item_planes(m, t, m->dim == 1 ? m->par[t] : 0);
+        if (s.kahan) k_prim_from_u<true><<<conv_grid(s.n), 256, 0, m->stream>>>(s, m->stage + off[t]);
+        else k_prim_from_u<false><<<conv_grid(s.n), 256, 0, m->stream>>>(s, m->stage + off[t]);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(prim, m->stage, sizeof(double) * off[m->nitems], cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    if (e != cudaSuccess) { snprintf(err, len, "state download failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     return SHLL_OK;
 }
 

@@ -57,7 +57,8 @@ EXPORTS = [
     "Free_Memory", "shll_ref_dt", "shll_checkpoint", "shll_restore", "shll_kernel_launches",
     "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
     "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
-    "shll_set_resident", "shll_debug_stall_chunk", "shll_batch_set_primitives",
+    "shll_set_resident", "shll_debug_stall_chunk", "shll_batch_set_primitives", "shll_initial_primitives",
+    "shll_batch_set_all_primitives", "shll_batch_get_all_primitives",
 ]
 
 
@@ -102,6 +103,9 @@ def lib():
         L.shll_batch_item_status.argtypes = [vp, ctypes.c_int]
         L.shll_batch_get_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
         L.shll_batch_set_primitives.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
+        L.shll_initial_primitives.argtypes = [P, dp, dp, dp, dp]
+        L.shll_batch_set_all_primitives.argtypes = [vp, dp]
+        L.shll_batch_get_all_primitives.argtypes = [vp, dp]
         L.shll_batch_totals.argtypes = [vp, ctypes.c_int, dp]
         L.shll_batch_cell_updates.argtypes = [vp]
         L.shll_batch_cell_updates.restype = ctypes.c_long
@@ -143,6 +147,21 @@ def params(dim=1, order=1, nx=256, ny=None, precision="f64", **kw):
 
 def steps_for(p):
     return lib().shll_steps_for(ctypes.byref(p))
+
+
+def initial_primitives(p, out=None):
+    """(nv, n) array: the initial rho, u, [v,] T of p's descriptor (what init_state loads), into
+    `out` (C-contiguous float64 of that shape) when given."""
+    nv = 4 if p.dim == 2 else 3
+    n = p.nx * (p.ny if p.dim == 2 else 1)
+    if out is None:
+        out = np.zeros((nv, n))
+    assert out.shape == (nv, n) and out.dtype == np.float64 and out.flags.c_contiguous
+    rc = lib().shll_initial_primitives(ctypes.byref(p), _dp(out[0]), _dp(out[1]), _dp(out[2]) if nv == 4 else None,
+                                       _dp(out[nv - 1]))
+    if rc != OK:
+        raise ShllError(rc, "initial_primitives: invalid parameters")
+    return out
 
 
 def kernel_launches():
@@ -333,6 +352,23 @@ class Batch:
         vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         return self._ck(lib().shll_batch_set_primitives(self.h, i, _dp(arrs[0]), _dp(arrs[1]), _dp(vv), _dp(arrs[2])),
                         "batch_set_primitives")
+
+    def packed_size(self):
+        """Doubles of the packed layout: item after item, each item's planes rho, u, [v,] T."""
+        return sum((4 if p.dim == 2 else 3) * p.nx * (p.ny if p.dim == 2 else 1) for p in self.items)
+
+    def set_all_primitives(self, packed):
+        """Every item's state from one packed host array (see packed_size)."""
+        assert packed.dtype == np.float64 and packed.flags.c_contiguous and packed.size == self.packed_size()
+        return self._ck(lib().shll_batch_set_all_primitives(self.h, _dp(packed)), "batch_set_all_primitives")
+
+    def get_all_primitives(self, out=None):
+        """Every item's primitives into one packed array (see packed_size)."""
+        if out is None:
+            out = np.zeros(self.packed_size())
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.packed_size()
+        self._ck(lib().shll_batch_get_all_primitives(self.h, _dp(out)), "batch_get_all_primitives")
+        return out
 
     def primitives(self, i, out=None):
         """(nv, n) array of item i: rho, u, [v,] T (into `out` when given, as Context.primitives)."""

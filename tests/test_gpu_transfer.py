@@ -101,3 +101,62 @@ def test_primitives_into_caller_buffer(shll):
     assert out is buf
     assert np.array_equal(buf, c.primitives())
     c.close()
+
+
+@pytest.mark.parametrize("dim", [1, 2])
+def test_rerun_from_uploaded_initial_state_is_identical(shll, dim):
+    # run; upload the descriptor's initial primitives again (shll_initial_primitives); run again:
+    # nothing of the first run may carry over into the second
+    if dim == 1:
+        p = shll.params(1, 2, nx=9000, precision="mixed_f64", n_steps=400)
+    else:
+        p = shll.params(2, 1, nx=96, ny=64, precision="mixed_f64", n_steps=150, ic_kind=shll.IC_CIRCLE2D,
+                        ic_cx=0.5, ic_cy=0.5, ic_radius=0.3, ic_rho_l=5.0, ic_T_l=1.2, ic_rho_r=1.0, ic_T_r=1.0)
+    c = shll.Context(p)
+    c.init_state()
+    init = c.primitives()
+    c.run()
+    first = c.primitives()
+    prim = shll.initial_primitives(p)
+    assert np.allclose(prim, init, rtol=1e-14, atol=0)   # (U -> P on the device rounds)
+    if dim == 1:
+        c.set_primitives(prim[0], prim[1], prim[2])
+    else:
+        c.set_primitives(prim[0], prim[1], prim[3], v=prim[2])
+    c.run()
+    assert np.array_equal(c.primitives(), first)
+    c.close()
+
+
+@pytest.mark.parametrize("dim", [1, 2])
+def test_batch_packed_transfers(shll, dim):
+    if dim == 1:
+        items = [shll.params(1, o, nx=n, precision="mixed_f64", n_steps=200, ic_rho_l=r)
+                 for o, n, r in ((1, 700, 3.0), (2, 1900, 8.0), (1, 2600, 20.0))]
+    else:
+        items = [shll.params(2, 1, nx=n, ny=n, precision="mixed_f64", n_steps=60, ic_kind=shll.IC_CIRCLE2D,
+                             ic_cx=0.5, ic_cy=0.5, ic_radius=0.2, ic_rho_l=r, ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0)
+                 for n, r in ((64, 4.0), (32, 9.0))]
+    b = shll.Batch(items)
+    b.run()
+    ref = [b.primitives(i) for i in range(len(items))]
+    packed = b.get_all_primitives()
+    off = 0
+    for i, p in enumerate(items):
+        size = ref[i].size
+        assert np.array_equal(packed[off:off + size].reshape(ref[i].shape), ref[i])
+        off += size
+    # re-upload every item's initial state at once and run again: the same results
+    init = np.concatenate([shll.initial_primitives(p).ravel() for p in items])
+    b.set_all_primitives(init)
+    b.run()
+    assert np.array_equal(b.get_all_primitives(), packed)
+    # a bad cell in the second item is refused before any state changes
+    bad = init.copy()
+    n0 = ref[0].size
+    bad[n0 + 7] = -1.0
+    with pytest.raises(shll.ShllError) as e:
+        b.set_all_primitives(bad)
+    assert e.value.status == shll.ERR_ARG and "item 1, cell 7" in str(e.value)
+    assert np.array_equal(b.get_all_primitives(), packed)
+    b.close()
