@@ -1658,6 +1658,23 @@ int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
                 if (B * F <= std::max(trial_steps, 128) && B <= MW / 16) cands.push_back({B, F, half});
     std::map<TuneKey, std::vector<int>> classes;
     for (int t = 0; t < m->nitems; t++) classes[tune_key(m->tubes[t], m->kahan)].push_back(t);
+    // per class, the longest sweep whose chunks (window MW minus the halos) still number at most one
+    // per SM for the class's largest tube: such a tube runs resident with every SM busy, and a longer
+    // sweep spreads the per-sweep cost (records, neighbour wait, halo loads) over more steps (65536
+    // cells, second order: 20 steps, 152 chunks of 431 cells)
+    for (auto& kv : classes) {
+        int nmax = 0, order = 1;
+        for (int t : kv.second) { nmax = std::max(nmax, m->tubes[t].n); order = m->tubes[t].order; }
+        const int per = (nmax + device_sms() - 1) / device_sms();
+        const int Bfit = (MW - per) / (2 * order);
+        if (Bfit > 8 && Bfit < MW / 16 && Bfit != 16)
+            for (int F : {1, 2, 4, 8})
+                if (Bfit * F <= std::max(trial_steps, 128)) {
+                    bool dup = false;
+                    for (const Cand& c : cands) dup = dup || (c.B == Bfit && c.F == F && c.half == 0);
+                    if (!dup) cands.push_back({Bfit, F, 0});
+                }
+    }
     auto set_class = [&](const std::vector<int>& ts, Cand c) {
         for (int t : ts) {
             TubeP& tp = m->tubes[t];

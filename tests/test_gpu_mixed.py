@@ -138,7 +138,7 @@ def test_autotune_batch_keeps_results_and_conservation(shll, oracle):
     b.autotune(256)
     chosen = [b.tuning(i) for i in range(len(items))]
     for sweep, fold, chunk in chosen:
-        assert sweep in (8, 16, 32) and fold % sweep == 0 and fold // sweep in (1, 2, 4, 8) and chunk > 0
+        assert 8 <= sweep <= 32 and fold % sweep == 0 and fold // sweep in (1, 2, 4, 8) and chunk > 0
     b.run()
     for i, n in enumerate(sizes):
         _, ref, _ = oracle.run(oracle.make_cfg(order=1, nx=n), oracle.ic_sod(n))
@@ -153,7 +153,7 @@ def test_autotune_single_tube(shll, oracle):
     c.init_state()
     c.autotune(256)
     sweep, fold, chunk = c.tuning()
-    assert sweep in (8, 16, 32) and chunk > 0
+    assert 8 <= sweep <= 32 and chunk > 0
     c.run()
     _, ref, _ = oracle.run(oracle.make_cfg(order=2, nx=1024), oracle.ic_sod(1024))
     assert np.max(np.mean(np.abs(c.primitives() - ref), axis=1)) <= 1e-6
