@@ -23,7 +23,7 @@ if [ ! -f "$REF/base-c/base_shll.c" ]; then
     exit 0
 fi
 mkdir -p "$OUT"
-TMP=$(mktemp -d)
+TMP=$(mktemp -d "$OUT/tmp.XXXXXX")
 trap 'rm -rf "$TMP"' EXIT
 
 # patch <src> <dst> <prec:32|64> <sed expressions...>
