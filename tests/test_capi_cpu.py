@@ -84,3 +84,20 @@ def test_status_strings(shll):
 def test_batch_rejects_empty(shll):
     h = ctypes.c_void_p()
     assert shll.lib().shll_batch_create(None, 0, ctypes.byref(h)) == shll.ERR_ARG
+
+
+def test_initial_primitives_match_the_oracle(shll, oracle):
+    # host-side initial conditions (what shll_init_state loads), no device involved
+    import numpy as np
+    p = shll.params(1, 1, nx=1000, precision="mixed_f64")
+    assert np.array_equal(shll.initial_primitives(p), oracle.ic_sod(1000))
+    p = shll.params(1, 2, nx=777, precision="f64", ic_x_d=0.37, ic_rho_l=4.5, ic_T_l=1.7)
+    assert np.array_equal(shll.initial_primitives(p), oracle.ic_sod(777, x_d=0.37, rhoL=4.5, TL=1.7))
+    p = shll.params(2, 1, nx=40, ny=24, precision="f64")
+    assert np.array_equal(shll.initial_primitives(p), oracle.ic_ref_box2d(40, 24))
+    p = shll.params(2, 1, nx=64, ny=48, precision="mixed_f64", ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5, ic_cy=0.5,
+                    ic_radius=0.3, ic_rho_l=7.0, ic_T_l=1.3, ic_rho_r=1.0, ic_T_r=1.0)
+    assert np.array_equal(shll.initial_primitives(p),
+                          oracle.ic_circle2d(64, 48, r=0.3, rho_in=7.0, T_in=1.3, rho_out=1.0, T_out=1.0))
+    with pytest.raises(shll.ShllError):
+        shll.initial_primitives(shll.params(1, 1, nx=0))
