@@ -126,3 +126,39 @@ def test_resident_wait_runs_out_and_is_reported(shll):
         shll.debug_stall_chunk(-1)
     out, _, launches = _ctx_run(shll, p, [16 * 10], resident=True)
     assert launches == 2 and np.isfinite(out).all()
+
+
+def test_tuned_sod_tube_resident_equals_launch_per_sweep(shll, oracle):
+    # the benchmark's configuration: 65536 cells, second order, autotuned (the longest sweep whose
+    # chunks fit one per SM); the resident run and the launch-per-sweep run of the same tuned
+    # chunks give the same bits, close to the exact Riemann solution, with mass conserved
+    n = 65536
+    p = shll.params(1, 2, nx=n, precision="mixed_f64")
+    a = shll.Context(p)
+    a.init_state()
+    a.autotune()
+    choice = a.tuning()
+    assert 8 <= choice[0] <= 32 and choice[2] > 0
+    t0 = a.totals()
+    n0 = shll.kernel_launches()
+    steps = a.run()
+    resident_launches = shll.kernel_launches() - n0
+    t1 = a.totals()
+    shll.set_resident(False)
+    try:
+        b = shll.Context(p)   # picks up the tuned choice of this size class
+        b.init_state()
+        assert b.tuning() == choice
+        n0 = shll.kernel_launches()
+        b.run()
+        assert shll.kernel_launches() - n0 > 1000
+    finally:
+        shll.set_resident(True)
+    if (n + choice[2] - 1) // choice[2] <= 152:   # (its chunks fit the 152 SMs at once: one launch + fix-up)
+        assert resident_launches == 2
+    assert np.array_equal(a.primitives(), b.primitives())
+    ex = oracle.riemann_exact(n, steps * (0.125 / n))
+    assert np.mean(np.abs(a.primitives()[0] - ex[0])) < 0.003
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+    a.close()
+    b.close()
