@@ -225,8 +225,11 @@ int shll_batch_restore(shll_batch* b);
  * SHLL_PREC_MIXED_F64 arithmetic of shll_step, on `stream` (a cudaStream_t, NULL = default).
  * All other memory it needs lives in one 2 MiB array inside the library, which every GPU that
  * loads the library holds until the process exits; so p->nx is limited to 65536 cells (larger
- * tubes are rejected with SHLL_ERR_ARG), p->dim must be 1 and p->precision MIXED_F64.  The first
+ * tubes are rejected with SHLL_ERR_ARG), p->dim must be 1 and p->precision MIXED_F64, and the
+ * other parameters pass the same checks as in shll_create (SHLL_ERR_ARG otherwise).  The first
  * call on each device looks up that array's device address: make it before any stream capture.
+ * The address is kept for the life of the process, so do not call this entry point again on a
+ * device after cudaDeviceReset() (which unloads the library's device image).
  * Every call uses the same array and leaves its contents behind, so calls that overlap on the
  * GPU (other threads, other streams) race with each other; serialise them.  Returns after the
  * work has completed. */

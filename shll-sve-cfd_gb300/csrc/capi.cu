@@ -91,7 +91,7 @@ extern "C" void shll_params_default(shll_params* p, int dim, int order) {
     }
 }
 
-static int validate(const shll_params* p, char* err, size_t len) {
+int shll_validate_params(const shll_params* p, char* err, size_t len) {
     if (!p) { snprintf(err, len, "params is NULL"); return SHLL_ERR_ARG; }
     if (p->dim != 1 && p->dim != 2) { snprintf(err, len, "dim must be 1 or 2 (got %d)", p->dim); return SHLL_ERR_ARG; }
     if (p->order != 1 && p->order != 2) { snprintf(err, len, "order must be 1 or 2 (got %d)", p->order); return SHLL_ERR_ARG; }
@@ -108,6 +108,10 @@ static int validate(const shll_params* p, char* err, size_t len) {
         return SHLL_ERR_ARG;
     }
     if (p->limiter != 0 && p->limiter != 1) { snprintf(err, len, "limiter must be 0 or 1"); return SHLL_ERR_ARG; }
+    if (p->order == 2 && p->limiter == 1 && !(p->mc_alpha > 0.0 && p->mc_alpha <= 2.0)) {
+        snprintf(err, len, "MC limiter alpha must lie in (0, 2] (got %g)", p->mc_alpha);
+        return SHLL_ERR_ARG;
+    }
     if (p->fold_steps < 0) { snprintf(err, len, "fold_steps must be >= 0"); return SHLL_ERR_ARG; }
     int k = p->ic.kind;
     if (k < SHLL_IC_SOD || k > SHLL_IC_QUADRANTS2D) { snprintf(err, len, "unknown initial condition %d", k); return SHLL_ERR_ARG; }
@@ -155,7 +159,7 @@ static long count_steps_t(const shll_params* p) {
 
 extern "C" long shll_steps_for(const shll_params* p) {
     char e[128];
-    if (validate(p, e, sizeof(e)) != SHLL_OK) return -1;
+    if (shll_validate_params(p, e, sizeof(e)) != SHLL_OK) return -1;
     if (p->n_steps > 0) return p->n_steps;
     return clock_is_f32(p) ? count_steps_t<float>(p) : count_steps_t<double>(p);
 }
@@ -239,7 +243,7 @@ extern "C" int shll_create(const shll_params* p, shll_ctx** out) {
     if (!out) return SHLL_ERR_ARG;
     *out = nullptr;
     char e[256];
-    int rc = validate(p, e, sizeof(e));
+    int rc = shll_validate_params(p, e, sizeof(e));
     if (rc != SHLL_OK) {
         fprintf(stderr, "shll_create: %s\n", e);
         return rc;
@@ -389,7 +393,7 @@ extern "C" int shll_init_state(shll_ctx* c) {
 extern "C" int shll_initial_primitives(const shll_params* p, double* rho, double* u, double* v, double* T) {
     char e[256];
     if (!p || !rho || !u || !T || (p->dim == 2 && !v)) return SHLL_ERR_ARG;
-    if (validate(p, e, sizeof(e)) != SHLL_OK || p->ic.kind == SHLL_IC_USER) return SHLL_ERR_ARG;
+    if (shll_validate_params(p, e, sizeof(e)) != SHLL_OK || p->ic.kind == SHLL_IC_USER) return SHLL_ERR_ARG;
     const size_t n = (size_t)p->nx * (p->dim == 2 ? p->ny : 1);
     const int nv = p->dim == 2 ? 4 : 3;
     std::vector<double> prim((size_t)nv * n);
@@ -643,7 +647,7 @@ static shll_ctx* g_ref = nullptr;
 
 extern "C" int shll_ref_configure(const shll_params* p) {
     char e[256];
-    int rc = validate(p, e, sizeof(e));
+    int rc = shll_validate_params(p, e, sizeof(e));
     if (rc != SHLL_OK) { fprintf(stderr, "shll_ref_configure: %s\n", e); return rc; }
     g_ref_params = *p;
     g_ref_configured = true;
@@ -713,7 +717,7 @@ extern "C" int shll_batch_create(const shll_params* items, int count, shll_batch
     *out = nullptr;
     char e[256];
     for (int i = 0; i < count; i++) {
-        int rc = validate(&items[i], e, sizeof(e));
+        int rc = shll_validate_params(&items[i], e, sizeof(e));
         if (rc != SHLL_OK) { fprintf(stderr, "shll_batch_create: item %d: %s\n", i, e); return rc; }
         if (items[i].ic.kind == SHLL_IC_USER) {
             fprintf(stderr, "shll_batch_create: item %d: batches take descriptor initial conditions\n", i);

@@ -1876,7 +1876,8 @@ constexpr size_t kStaticStateBytes = (size_t)3 * kStaticMaxCells * sizeof(double
 constexpr size_t kStaticBSumOff = kStaticStateBytes;                                  // 2 x BSum[256]
 constexpr size_t kStaticChunkOff = kStaticBSumOff + 2 * kStaticMaxChunks * sizeof(BSum);
 constexpr size_t kStaticTubeOff = (kStaticChunkOff + kStaticMaxChunks * sizeof(Chunk) + 255) / 256 * 256;
-constexpr size_t kStaticFlagOff = kStaticTubeOff + 256;
+constexpr size_t kStaticFlagOff = kStaticTubeOff + (sizeof(TubeP) + 255) / 256 * 256;
+static_assert(kStaticFlagOff >= kStaticTubeOff + sizeof(TubeP), "the tube descriptor overlaps the error flag");
 constexpr size_t kStaticScratchBytes = 2u << 20;
 static_assert(kStaticFlagOff + 256 <= kStaticScratchBytes, "static scratch layout exceeds its array");
 constexpr int kStaticMaxDevices = 64;
@@ -1915,6 +1916,13 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     if (!p || !d_cons) {
         fprintf(stderr, "shll_tube_run_static: params and state buffer are required\n");
         return SHLL_ERR_ARG;
+    }
+    {   // the same parameter checks as shll_create, whatever nsteps is
+        char msg[256];
+        if (shll_validate_params(p, msg, sizeof(msg)) != SHLL_OK) {
+            fprintf(stderr, "shll_tube_run_static: %s\n", msg);
+            return SHLL_ERR_ARG;
+        }
     }
     if (p->dim != 1 || (p->order != 1 && p->order != 2) || p->precision != SHLL_PREC_MIXED_F64) {
         fprintf(stderr, "shll_tube_run_static: takes one 1D tube (order 1 or 2) in SHLL_PREC_MIXED_F64\n");

@@ -1,12 +1,17 @@
 // Internal declarations shared by the CUDA translation units of libshll_gb300.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstddef>
 #include <cstdint>
 
 // device error flags (bitwise OR into one int per context)
 #define SHLL_FLAG_NONPOSITIVE 1   // density or temperature <= 0 (or NaN) seen
 #define SHLL_FLAG_TIMEOUT 2       // a bounded device-side wait gave up
 #define SHLL_FLAG_BADARG 4        // a kernel rejected its launch arguments
+
+struct shll_params;
+// the parameter checks of shll_create (SHLL_OK, or SHLL_ERR_ARG with a message in err)
+int shll_validate_params(const shll_params* p, char* err, size_t len);
 
 // kernel launches issued by the library (shll_kernel_launches)
 void shll_count_launches(long n);

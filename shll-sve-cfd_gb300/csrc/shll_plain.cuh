@@ -13,6 +13,9 @@
 // touches it); with REAL = double it is a no-op.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <algorithm>
+
 #include "shll_internal.h"
 
 namespace SHLL_PLAIN_NS {
@@ -317,8 +320,8 @@ __global__ void __launch_bounds__(TI * TJ) k_step2(const REAL* __restrict__ Uin,
 // ---------------- staged kernels (the reference's separate stages) ----------------
 // Compute_U_from_P: base_shll.c:76-80 / base_shll_2d.c:126-131.  P: nv planes (+ a plane).
 template <typename REAL>
-__global__ void k_u_from_p(const REAL* __restrict__ P, REAL* __restrict__ U, int n, int dim, Gas<REAL> g) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+__global__ void k_u_from_p(const REAL* __restrict__ P, REAL* __restrict__ U, long n, int dim, Gas<REAL> g) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
         if (dim == 1) {
             REAL p0 = P[c], p1 = P[n + c], p2 = P[2 * n + c];
             U[c] = p0; U[n + c] = p0 * p1;
@@ -333,10 +336,10 @@ __global__ void k_u_from_p(const REAL* __restrict__ P, REAL* __restrict__ U, int
 
 // Compute_P_from_U: P planes rho, u, [v,] T and the sound-speed plane a after them.
 template <typename REAL>
-__global__ void k_p_from_u(const REAL* __restrict__ U, REAL* __restrict__ P, int n, int dim, Gas<REAL> g,
+__global__ void k_p_from_u(const REAL* __restrict__ U, REAL* __restrict__ P, long n, int dim, Gas<REAL> g,
                            int* __restrict__ flag) {
     int bad = 0;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
         if (dim == 1) {
             REAL u0 = U[c], p1, p2, a;
             prim1(g, u0, U[n + c], U[2 * n + c], p1, p2, a);
@@ -355,9 +358,9 @@ __global__ void k_p_from_u(const REAL* __restrict__ U, REAL* __restrict__ P, int
 // Compute_F_from_P from the stored P (and its a plane) and U, as the reference reads both.
 template <typename REAL>
 __global__ void k_f_from_p(const REAL* __restrict__ U, const REAL* __restrict__ P, REAL* __restrict__ fp,
-                           REAL* __restrict__ fm, REAL* __restrict__ hp, REAL* __restrict__ hm, int n, int dim,
+                           REAL* __restrict__ fm, REAL* __restrict__ hp, REAL* __restrict__ hm, long n, int dim,
                            Gas<REAL> g) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
         if (dim == 1) {
             REAL a[3], b[3];
             flux1(g, U[c], U[n + c], U[2 * n + c], P[n + c], P[2 * n + c], P[3 * n + c], a, b);
@@ -378,9 +381,10 @@ template <typename REAL>
 __global__ void k_update_staged(REAL* __restrict__ U, const REAL* __restrict__ fp, const REAL* __restrict__ fm,
                                 const REAL* __restrict__ hp, const REAL* __restrict__ hm, int nx, int ny, int dim,
                                 int order, Gas<REAL> g) {
-    const int n = nx * ny, nv = dim == 2 ? 4 : 3, sx_ = ny;  // x stride (1D: ny = 1)
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-        const int i = c / ny, j = c % ny;
+    const long n = (long)nx * ny;
+    const int nv = dim == 2 ? 4 : 3, sx_ = ny;  // x stride (1D: ny = 1)
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c / ny), j = (int)(c % ny);
         for (int k = 0; k < nv; k++) {
             const REAL* Fp = fp + k * n; const REAL* Fm = fm + k * n;
             REAL u = U[k * n + c];
@@ -401,7 +405,7 @@ __global__ void k_update_staged(REAL* __restrict__ U, const REAL* __restrict__ f
                     u = u - g.DT_ON_DY * (Hp[c] - Hm[c] + Tt - B);
                 }
             } else {
-                auto sl = [&](const REAL* f, int cc, int ii, int st, int nn) -> REAL {
+                auto sl = [&](const REAL* f, long cc, int ii, int st, int nn) -> REAL {
                     if (ii <= 0 || ii >= nn - 1) return (REAL)0;
                     return slope(g, f[cc - st], f[cc], f[cc + st]);
                 };
@@ -464,10 +468,9 @@ template <typename REAL>
 static cudaError_t stage_t(const PlainArgs& a, int which) {
     shll_count_launches(1);
     Gas<REAL> g = make_gas<REAL>(a);
-    const int n = a.nx * (a.dim == 2 ? a.ny : 1);
+    const long n = (long)a.nx * (a.dim == 2 ? a.ny : 1);
     const int threads = 256;
-    int blocks = (n + threads - 1) / threads;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    int blocks = (int)std::min<long>((n + threads - 1) / threads, 152L * 16);
     REAL* U = static_cast<REAL*>(a.Uout);
     REAL* P = static_cast<REAL*>(a.P);
     switch (which) {

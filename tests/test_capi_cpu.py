@@ -101,3 +101,25 @@ def test_initial_primitives_match_the_oracle(shll, oracle):
                           oracle.ic_circle2d(64, 48, r=0.3, rho_in=7.0, T_in=1.3, rho_out=1.0, T_out=1.0))
     with pytest.raises(shll.ShllError):
         shll.initial_primitives(shll.params(1, 1, nx=0))
+
+
+@pytest.mark.parametrize("field,value", [("gamma", 1.0), ("cfl", 0.0), ("R", 0.0), ("limiter", 2),
+                                         ("mc_alpha", 0.0), ("fold_steps", -1), ("nx", 1)])
+def test_static_tube_entry_validates_parameters_for_any_step_count(shll, field, value):
+    # shll_tube_run_static applies shll_create's checks also when the caller gives the step count;
+    # they come before any CUDA call, so a stand-in device pointer is never touched here
+    L = shll.lib()
+    L.shll_tube_run_static.argtypes = [ctypes.POINTER(shll.Params), ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p]
+    L.shll_tube_run_static.restype = ctypes.c_int
+    p = shll.params(1, 2, nx=1024, precision="mixed_f64", limiter=1, mc_alpha=1.25)
+    setattr(p, field, value)
+    for nsteps in (100, 0):
+        assert L.shll_tube_run_static(ctypes.byref(p), ctypes.c_void_p(4096), nsteps, None) == shll.ERR_ARG
+
+
+def test_mc_limiter_alpha_is_checked(shll):
+    h = ctypes.c_void_p()
+    p = shll.params(1, 2, limiter=1, mc_alpha=3.0)
+    assert shll.lib().shll_create(ctypes.byref(p), ctypes.byref(h)) == shll.ERR_ARG
+    p = shll.params(1, 2, limiter=1, mc_alpha=float("nan"))
+    assert shll.steps_for(p) == -1

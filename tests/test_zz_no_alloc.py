@@ -72,3 +72,16 @@ def test_static_entry_rejects_oversized_tube(shll):
     L.shll_tube_run_static.argtypes = [ctypes.POINTER(shll.Params), ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p]
     L.shll_tube_run_static.restype = ctypes.c_int
     assert L.shll_tube_run_static(ctypes.byref(p), ctypes.c_void_p(buf.data_ptr()), 10, None) == shll.ERR_ARG
+
+
+def test_static_entry_validates_parameters_with_explicit_steps(shll):
+    torch = pytest.importorskip("torch")
+    buf = torch.zeros(3 * 1024, dtype=torch.float64, device="cuda")
+    L = shll.lib()
+    L.shll_tube_run_static.argtypes = [ctypes.POINTER(shll.Params), ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p]
+    L.shll_tube_run_static.restype = ctypes.c_int
+    for field, value in (("gamma", 1.0), ("cfl", 0.0), ("limiter", 3)):
+        p = shll.params(1, 1, nx=1024, precision="mixed_f64")
+        setattr(p, field, value)
+        assert L.shll_tube_run_static(ctypes.byref(p), ctypes.c_void_p(buf.data_ptr()), 50, None) == shll.ERR_ARG
+    assert torch.count_nonzero(buf).item() == 0   # refused before any work on the buffer
