@@ -168,8 +168,9 @@ int shll_save_results(shll_ctx* ctx, const char* path);
 /* ---- batches of independent tubes / domains ---- */
 typedef struct shll_batch shll_batch;
 /* items: count parameter sets (all dim 1, or all dim 2, any sizes/orders/initial data), all
- * with one precision: SHLL_PREC_F64 (the plain FP64 arithmetic, one launch per time step over
- * every item) or a MIXED mode (the sweep engine in 1D; first order only in 2D). */
+ * with one precision: SHLL_PREC_F64 or SHLL_PREC_F64_EXACT (the plain FP64 arithmetic, with or
+ * without fused multiply-add, one launch per time step over every item) or a MIXED mode (the
+ * sweep engine in 1D; first order only in 2D).  SHLL_PREC_F32_EXACT batches: SHLL_ERR_UNSUPPORTED. */
 int shll_batch_create(const shll_params* items, int count, shll_batch** out);
 /* Runs every item to its own end (its own DT and step count). */
 int shll_batch_run(shll_batch* b);
@@ -253,6 +254,17 @@ void shll_set_graph_replay(int on);
  * to the one-launch-per-sweep schedule.  on = 0 selects that schedule for every run (default 1;
  * process-wide).  A wait that gives up makes the run return SHLL_ERR_TIMEOUT. */
 void shll_set_resident(int on);
+
+/* Pair flux of first-order mixed-precision 1D runs (no counterpart in the reference): where the
+ * flow is supersonic, the reference scheme (base-c/base_shll.c:130-159, whose split gives the
+ * u - a wave the negative numerical viscosity a(1 - M)/2 once M > 1) amplifies every per-step
+ * rounding error by orders of magnitude.  So a chunk of cells whose own or neighbouring cells
+ * exceeded Mach 0.6 at the end of a sweep (or, at the start of a run, held a pressure jump of more
+ * than 1.5 times) evaluates its split fluxes, interface sums and increments of the next sweep in
+ * double-FP32 arithmetic (pairs of FP32 numbers, about 48 significant bits) instead of FP32.
+ * on = 0 keeps FP32 everywhere, on = 2 uses the pair flux in every chunk of every first-order
+ * tube (default 1; process-wide). */
+void shll_set_pair_flux(int on);
 
 /* Test hook (no counterpart in the reference): in resident runs the chunk with this index (chunks
  * are numbered along the tubes from 0) never publishes its progress, so its neighbours' bounded

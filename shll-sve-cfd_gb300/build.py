@@ -26,8 +26,10 @@ UNITS = {
     "mixed2d.cu": ["-fmad=false"],
     "reduce.cu": [],
     "plain_batch.cu": [],
+    "plain_batch_exact.cu": ["-fmad=false"],
 }
-HEADERS = ["shll_internal.h", "shll_plain.cuh", "mixed.h", "mixed_common.cuh", "plain_batch.h"]
+HEADERS = ["shll_internal.h", "shll_plain.cuh", "mixed.h", "mixed_common.cuh", "plain_batch.h",
+           "plain_batch_kernels.cuh"]
 
 
 def _stale(target, deps):

@@ -705,7 +705,7 @@ extern "C" double shll_ref_dt(void) { return g_ref ? g_ref->DT : 0.0; }
 // ---------------- batches ----------------
 struct shll_batch {
     MixedState* m = nullptr;     // mixed-precision items
-    PlainBatch* pb = nullptr;    // SHLL_PREC_F64 items (one launch per step)
+    PlainBatch* pb = nullptr;    // SHLL_PREC_F64 / F64_EXACT items (one launch per step)
     cudaStream_t stream = nullptr;
     int count = 0;
     bool loaded = false;
@@ -724,12 +724,22 @@ extern "C" int shll_batch_create(const shll_params* items, int count, shll_batch
             return SHLL_ERR_ARG;
         }
     }
+    const int prec = items[0].precision;
+    for (int i = 1; i < count; i++)
+        if (items[i].precision != prec || items[i].dim != items[0].dim) {
+            fprintf(stderr, "shll_batch_create: item %d: batch items share one dimension and one precision\n", i);
+            return SHLL_ERR_ARG;
+        }
+    if (prec == SHLL_PREC_F32_EXACT) {
+        fprintf(stderr, "shll_batch_create: batches take F64, F64_EXACT or the mixed precisions\n");
+        return SHLL_ERR_UNSUPPORTED;
+    }
     shll_batch* b = new (std::nothrow) shll_batch();
     if (!b) return SHLL_ERR_NOMEM;
     b->count = count;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { delete b; return SHLL_ERR_CUDA; }
     int rc;
-    if (items[0].precision == SHLL_PREC_F64) {
+    if (prec == SHLL_PREC_F64 || prec == SHLL_PREC_F64_EXACT) {
         b->pb = plain_batch_create(items, count, b->stream, b->err, sizeof(b->err));
         if (!b->pb) {
             fprintf(stderr, "shll_batch_create: %s\n", b->err);

@@ -64,6 +64,7 @@ struct TubeP {
     int B;            // steps per sweep (temporal blocking depth, <= MW / 16)
     int fold_sweeps;  // sweeps per fold window (FP64 state read at the first, written at the last)
     int owned;        // owned cells per chunk (0: the window minus the halos)
+    float gg1p[2], gm1p[2];  // gamma (gamma-1) and gamma-1 = R/CV as FP32 pairs (pair flux)
 };
 
 struct Chunk {
@@ -156,7 +157,30 @@ struct SweepArgs {
     int* flag;
     int* item_flags;    // per tube (may be null)
     int stall_id;       // resident runs, test hook: this chunk never publishes its progress (-1: none)
+    // first order: per chunk id and sweep parity, 1 if an owned cell's Mach number exceeded
+    // kPairMach at the end of that sweep; a chunk's sweep uses the pair flux when it or a
+    // neighbour had one at the end of the previous sweep.  Null: FP32 flux throughout.
+    int* mode[2];
+    float pair_m2;      // the squared Mach number that sets a flag (negative: every chunk, a test hook)
 };
+
+// Mach number above which a first-order chunk and its neighbours evaluate their fluxes in
+// double-FP32 arithmetic (the reference scheme amplifies rounding errors where M > 1; the margin
+// also covers cells that accelerate past M = 1 during the next sweep, and subsonic cells whose
+// FP32 rounding errors the flow carries into the supersonic region)
+constexpr float kPairMach = 0.6f;
+// dynamic shared memory of a pair-flux sweep: the remainders of the split fluxes
+constexpr int kPairSmem = 2 * 2 * 3 * MW * (int)sizeof(float);
+
+// the pair-flux decision for a chunk's sweep `sweep` (flags of the previous sweep, or of the
+// state at the start of the run for sweep 0); L2 loads, as the flags are written by other blocks
+__device__ __forceinline__ bool pair_mode(const SweepArgs& A, const Chunk& ch, int sweep) {
+    const int* f = ((sweep - 1) & 1) ? A.mode[1] : A.mode[0];
+    int v = __ldcg(f + ch.id);
+    if (ch.idL >= 0) v |= __ldcg(f + ch.idL);
+    if (ch.idR >= 0) v |= __ldcg(f + ch.idR);
+    return v != 0;
+}
 
 // correction owed to the first owned cell of the chunk with id `right` by its left neighbour
 // `left` for the sweep whose sums are in bs: lam*sum(F_left) - lam*sum(F_right) at their interface
@@ -193,14 +217,18 @@ __device__ __forceinline__ T ldx(const T* p) {
 // The double buffer makes the second barrier of a store/load/store pattern unnecessary: a
 // thread can only overwrite a buffer after every thread has passed the barrier that follows
 // the last reads of it.
+// FF: first order only, the split fluxes, interface sums and accumulation in double-FP32
+// arithmetic (flux1x2_ff); a launch of either form leaves the chunks whose pair-flux decision
+// (pair_mode) calls for the other form to the other launch of the same sweep.
 // RES: called by the resident kernel (k_tube1d), which keeps the frame and the neighbour-frame
 // offsets in shared memory for a whole fold window.  reuse: the owned cells' deviation pairs are
 // taken from dh/dl (this thread's registers after the previous sweep of the same geometry)
 // instead of memory; keep: the next sweep will do so, so only the cells that the neighbours read
 // as halo are stored.
-template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, bool RES>
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, bool RES, bool FF = false>
 __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch, const TubeP& tp, Smem1& S,
                             float2 (&dh)[3], float2 (&dl)[3], const bool reuse, const bool keep) {
+    static_assert(!FF || ORDER == 1, "the pair flux covers the first-order scheme");
     constexpr int R_ = ORDER;  // stencil reach per step
     Frame1& fr = S.fr;
 
@@ -235,6 +263,8 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
     if (!RES) {
         asm volatile("griddepcontrol.wait;" ::: "memory");
         asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+        // (block-uniform: every thread reads the same flags)
+        if (ORDER == 1 && A.mode[0] && pair_mode(A, ch, sweep) != FF) return;
     }
     // (selects rather than indexing the parameter arrays, which would copy them to local memory)
     const void* hin = inb ? A.hi[1] : A.hi[0];
@@ -414,6 +444,85 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
     const bool any_rec = rin0 || rin1 || rout0 || rout1;
     const int jl = max(w0 - 2, 0), jr = min(w0 + 2, MW - 2);  // neighbour pairs (clamped)
 
+    if constexpr (FF) {
+        // The same step in double-FP32 arithmetic: each cell's state U = U* + (dh + dl) as a pair,
+        // its physical split fluxes as pairs (values in S.sfp / S.sfm, remainders in dynamic
+        // shared memory), and the increment lam (F_{j-1/2} - F_{j+1/2}) of the full interface fluxes
+        // added to the deviation pair with a renormalising sum.  Reflective walls (first order):
+        // the wall flux (0, 2 fm1_0, 0) at cell 0 and (0, 2 fp1_{n-1}, 0) at cell n-1
+        // (base-c/base_shll.c:93-110); the boundary records keep the FP32 form's meaning,
+        // lam (F - Fref).
+        extern __shared__ __align__(16) float g_pair_smem[];
+        float* sfpl = g_pair_smem;               // [2][3][MW]
+        float* sfml = g_pair_smem + 2 * 3 * MW;  // [2][3][MW]
+        auto at = [](float* base, int b, int k, int w) { return reinterpret_cast<float2*>(base + (b * 3 + k) * MW + w); };
+        const FF2 gg1 = ffv(tp.gg1p[0], tp.gg1p[1]), gm1 = ffv(tp.gm1p[0], tp.gm1p[1]);
+        for (int s = 0; s < steps; s++) {
+            const int b = s & 1;
+            FF2 fp[3], fm[3];
+            {
+                FF2 U[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const FF2 d = ffnorm(dh[k], dl[k]);
+                    dh[k] = d.h;
+                    dl[k] = d.l;
+                    U[k] = ffadd(ffv(frp->Uh[k], frp->Ul[k]), d);
+                }
+                flux1x2_ff(U, gg1, gm1, fp, fm);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                *reinterpret_cast<float2*>(&S.sfp[b][k][w0]) = fp[k].h;
+                *reinterpret_cast<float2*>(&S.sfm[b][k][w0]) = fm[k].h;
+                *at(sfpl, b, k, w0) = fp[k].l;
+                *at(sfml, b, k, w0) = fm[k].l;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float2 pLh = *reinterpret_cast<const float2*>(&S.sfp[b][k][jl]);  // fp_{w0-2}, fp_{w0-1}
+                const float2 mRh = *reinterpret_cast<const float2*>(&S.sfm[b][k][jr]);  // fm_{w0+2}, fm_{w0+3}
+                const float2 pLl = *at(sfpl, b, k, jl), mRl = *at(sfml, b, k, jr);
+                const FF2 IN = ffadd_u({make_float2(pLh.y, fp[k].h.x), make_float2(pLl.y, fp[k].l.x)}, fm[k]);
+                const FF2 OUT = ffadd_u(fp[k], {make_float2(fm[k].h.y, mRh.x), make_float2(fm[k].l.y, mRl.x)});
+                FF2 tin, tout;
+                if (LAM_POW2) {  // lam a power of two (or 0 where masked): exact scaling
+                    tin = {mul2(lin2, IN.h), mul2(lin2, IN.l)};
+                    tout = {mul2(lout2, OUT.h), mul2(lout2, OUT.l)};
+                } else {
+                    tin = ffmul_u(IN, {lin2, llin2});
+                    tout = ffmul_u(OUT, {lout2, llout2});
+                }
+                FF2 v = ffadd({dh[k], dl[k]}, ffsub(tin, tout));
+                if (any_wall && k == 1) {  // (the wall's own interface is masked out of tin / tout)
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        if (!wallq[q]) continue;
+                        const bool left = ws + w0 + q == 0;
+                        const float sg = left ? 2.f : -2.f;  // + lam 2 fm1 at cell 0, - lam 2 fp1 at cell n-1
+                        const FF2 wf = {f2(sg * lane(left ? fm[1].h : fp[1].h, q)), f2(sg * lane(left ? fm[1].l : fp[1].l, q))};
+                        const FF2 t = LAM_POW2 ? ffscale(wf, lamh) : ffmul_u(wf, ffv(lamh, laml));
+                        const FF2 vq = ffadd({f2(lane(v.h, q)), f2(lane(v.l, q))}, t);
+                        set_lane(v.h, q, vq.h.x);
+                        set_lane(v.l, q, vq.l.x);
+                    }
+                }
+                dh[k] = v.h;
+                dl[k] = v.l;
+                if (any_rec) {  // lam (F - Fref) at the chunk's boundary interfaces
+                    float fh, fl;
+                    d2ff_bits(frp->F[k], fh, fl);
+                    const FF2 lref = LAM_POW2 ? ffscale(ffv(fh, fl), lamh) : ffmul(ffv(fh, fl), ffv(lamh, laml));
+                    const FF2 ri = ffsub(tin, lref), ro = ffsub(tout, lref);
+                    if (rin0) { S.rec[0][s][k][0] = ri.h.x; S.rec[0][s][k][1] = ri.l.x; }
+                    if (rin1) { S.rec[0][s][k][0] = ri.h.y; S.rec[0][s][k][1] = ri.l.y; }
+                    if (rout0) { S.rec[1][s][k][0] = ro.h.x; S.rec[1][s][k][1] = ro.l.x; }
+                    if (rout1) { S.rec[1][s][k][0] = ro.h.y; S.rec[1][s][k][1] = ro.l.y; }
+                }
+            }
+        }
+    } else
     for (int s = 0; s < steps; s++) {
         const int b = s & 1;
         // ---- split-flux deviations of both cells ----
@@ -523,6 +632,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
     // ---- fold the owned cells into the stored state (last sweep of a window), or pass their
     // deviation pairs to the next sweep ----
     int bad = 0;
+    int fast = 0;   // an owned cell above the pair-flux Mach number (first order)
     void* hout = outb ? A.hi[1] : A.hi[0];
     float* lout = outb ? A.lo[1] : A.lo[0];
     float* dhout = outb ? A.dh[1] : A.dh[0];
@@ -563,10 +673,18 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
         const float eint = __fadd_rn(uf[2], -__fmul_rn(0.5f, __fdividef(__fmul_rn(uf[1], uf[1]), uf[0])));
         // breakdown: non-positive density or internal energy, or an overflowed / NaN increment
         bad |= !(uf[0] > 0.f) || !(eint > 0.f) || !finite;
+        // M^2 = m^2 / (rho^2 a^2) with a^2 = gamma (gamma-1) eint / rho
+        if (ORDER == 1)
+            fast |= __fmul_rn(uf[1], uf[1]) >
+                    __fmul_rn(A.pair_m2, __fmul_rn(__fmul_rn(tp.gRf, tp.cvinvf), __fmul_rn(uf[0], eint)));
     }
     if (bad) {
         atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
         if (A.item_flags) atomicOr(&A.item_flags[ch.tube], SHLL_FLAG_NONPOSITIVE);
+    }
+    if (ORDER == 1 && A.mode[0]) {
+        const int any = __syncthreads_or(fast);
+        if (tid == 0) ((sweep & 1) ? A.mode[1] : A.mode[0])[ch.id] = any;
     }
 }
 
@@ -585,6 +703,62 @@ __global__ void __launch_bounds__(MT, 3) k_sweep1d(SweepArgs A) {
     float2 dh[3], dl[3];
     // (waits for the previous sweep inside)
     sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, false>(A, A.sweep, ch, tp, S, dh, dl, false, false);
+}
+
+// The pair-flux form of a first-order sweep, launched after the FP32 form for the same chunks
+// (each block runs its chunk only when the chunk's pair-flux decision calls for it).  Its own
+// kernel so that the longer double-FP32 step does not raise the register count, and so lower the
+// occupancy, of the FP32 sweeps.
+template <bool KAHAN, bool LAM_POW2>
+__global__ void __launch_bounds__(MT, 2) k_sweep1d_ff(SweepArgs A) {
+    __shared__ Smem1 S;
+    const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
+    const TubeP tp = A.tubes[ch.tube];
+    float2 dh[3], dl[3];
+    sweep_chunk<1, KAHAN, LAM_POW2, 0, false, true>(A, A.sweep, ch, tp, S, dh, dl, false, false);
+}
+
+// The pair-flux flags of the state at the start of a run (as sweep -1 would leave them): one block
+// per chunk.  A chunk is flagged when an owned cell exceeds the Mach threshold or when the
+// pressure within kJumpReach cells of its cells varies by more than the factor kPairJump: a gas at
+// rest at a diaphragm has M = 0, but the first sweep already accelerates it, and the FP32 rounding
+// of that sweep would be carried into the supersonic region that forms there.
+constexpr float kPairJump = 1.5f;
+constexpr int kJumpReach = 16;
+template <bool KAHAN>
+__global__ void __launch_bounds__(256) k_mode1d(SweepArgs A) {
+    __shared__ float wmax[8], wmin[8];
+    const Chunk ch = A.chunks[blockIdx.x];
+    const TubeP tp = A.tubes[ch.tube];
+    int fast = 0;
+    float pmax = 0.f, pmin = 3.0e38f;
+    if (tp.order == 1) {
+        const void* hin = tp.par ? A.hi[1] : A.hi[0];
+        const float* lin = tp.par ? A.lo[1] : A.lo[0];
+        const double g = tp.gamma * (tp.gamma - 1.0);
+        const int lo = max(0, ch.a - kJumpReach), hi = min(tp.n, ch.b + kJumpReach);
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+            const long idx = tp.base + i;
+            const double r = load_state<KAHAN>(hin, lin, idx);
+            const double m = load_state<KAHAN>(hin, lin, A.plane + idx);
+            const double E = load_state<KAHAN>(hin, lin, 2 * A.plane + idx);
+            const double eint = E - 0.5 * m * m / r;
+            if (i >= ch.a && i < ch.b) fast |= m * m > (double)A.pair_m2 * g * r * eint;
+            const float P = (float)(tp.RoCV * eint);
+            pmax = fmaxf(pmax, P);
+            pmin = fminf(pmin, P);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        pmax = fmaxf(pmax, __shfl_xor_sync(0xffffffffu, pmax, o));
+        pmin = fminf(pmin, __shfl_xor_sync(0xffffffffu, pmin, o));
+    }
+    if ((threadIdx.x & 31) == 0) { wmax[threadIdx.x >> 5] = pmax; wmin[threadIdx.x >> 5] = pmin; }
+    fast = __syncthreads_or(fast);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { pmax = fmaxf(pmax, wmax[w]); pmin = fminf(pmin, wmin[w]); }
+        A.mode[1][ch.id] = fast || (tp.order == 1 && pmax > kPairJump * pmin);
+    }
 }
 
 // polls of the neighbours' progress counters before a resident block gives up (under a second,
@@ -652,7 +826,16 @@ __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
         // sweeps of B steps inside a fold window share the geometry of the one before
         const bool reuse = sw % F != 0 && tp.steps - sw * tp.B >= tp.B;
         const bool keep = sw + 1 < nsw && (sw + 1) % F != 0 && tp.steps - (sw + 1) * tp.B >= tp.B;
-        sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+        if constexpr (ORDER == 1) {
+            // the neighbours' flags of the previous sweep are visible after the wait above (they
+            // were written before the neighbours' release); block-uniform
+            if (A.mode[0] && pair_mode(A, ch, sw))
+                sweep_chunk<1, KAHAN, LAM_POW2, LIM, true, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+            else
+                sweep_chunk<1, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+        } else {
+            sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+        }
         __syncthreads();
         // (the barrier orders the block's stores before thread 0's release at GPU scope)
         if (threadIdx.x == 0 && ch.id != A.stall_id) st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
@@ -722,7 +905,9 @@ static cudaError_t allow_solo_padding() {
         (const void*)k_sweep1d<2, false, true, 0>, (const void*)k_sweep1d<2, true, true, 0>,
         (const void*)k_sweep1d<2, false, false, 0>, (const void*)k_sweep1d<2, true, false, 0>,
         (const void*)k_sweep1d<2, false, true, 1>, (const void*)k_sweep1d<2, true, true, 1>,
-        (const void*)k_sweep1d<2, false, false, 1>, (const void*)k_sweep1d<2, true, false, 1>};
+        (const void*)k_sweep1d<2, false, false, 1>, (const void*)k_sweep1d<2, true, false, 1>,
+        (const void*)k_sweep1d_ff<false, true>, (const void*)k_sweep1d_ff<true, true>,
+        (const void*)k_sweep1d_ff<false, false>, (const void*)k_sweep1d_ff<true, false>};
     for (const void* k : ks) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSoloSmem);
         if (e != cudaSuccess) return e;
@@ -749,6 +934,32 @@ static cudaError_t launch_sweep(int variant, bool kahan, int grid, cudaStream_t 
         default: return launch_one<2, true, false, 1>(grid, s, A, pdl);
     }
 }
+
+// the pair-flux sweep of a first-order variant group (variants 0, 1); its dynamic shared memory
+// holds the remainders of the split fluxes (within the padding when the grid is a single wave)
+template <bool KAHAN, bool LAM_POW2>
+static cudaError_t launch_one_ff(int grid, cudaStream_t s, const SweepArgs& A, bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(MT);
+    cfg.dynamicSmemBytes = pdl && grid <= device_sms() ? kSoloSmem : kPairSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_sweep1d_ff<KAHAN, LAM_POW2>, A);
+}
+static cudaError_t launch_sweep_ff(int variant, bool kahan, int grid, cudaStream_t s, const SweepArgs& A, bool pdl) {
+    switch (variant * 2 + (kahan ? 1 : 0)) {
+        case 0: return launch_one_ff<false, true>(grid, s, A, pdl);
+        case 1: return launch_one_ff<true, true>(grid, s, A, pdl);
+        case 2: return launch_one_ff<false, false>(grid, s, A, pdl);
+        default: return launch_one_ff<true, false>(grid, s, A, pdl);
+    }
+}
+static_assert(kPairSmem <= kSoloSmem, "the pair-flux buffers fit in the padding of single-wave sweeps");
 
 // resident form of a run (k_tube1d): a cooperative launch of one block per chunk, each alone on
 // its SM (the same shared-memory padding as single-wave sweeps)
@@ -850,6 +1061,7 @@ struct MixedState {
     float* dh[2] = {nullptr, nullptr};   // deviation pairs between the sweeps of a fold window
     float* dl[2] = {nullptr, nullptr};
     Frame1* frames = nullptr;            // per chunk: frame of the current fold window
+    int* mode[2] = {nullptr, nullptr};   // per chunk, by sweep parity: pair-flux flags (first order)
     unsigned* prog = nullptr;            // per chunk: sweeps completed in a resident run
     size_t prog_n = 0;
     double* stage = nullptr;             // device staging of one item's primitive planes
@@ -945,6 +1157,20 @@ static void fix_fold_sweeps(MixedState* m) {
         if (min_owned[t] < m->tubes[t].order * m->tubes[t].B) m->tubes[t].fold_sweeps = 1;
 }
 
+// pair-flux flags per chunk and sweep parity, when a tube is first order
+static cudaError_t alloc_mode_flags(MixedState* m) {
+    for (int b = 0; b < 2; b++) { cudaFree(m->mode[b]); m->mode[b] = nullptr; }
+    bool first = false;
+    for (const TubeP& tp : m->tubes) first = first || tp.order == 1;
+    if (!first) return cudaSuccess;
+    for (int b = 0; b < 2; b++) {
+        cudaError_t e = cudaMalloc(&m->mode[b], sizeof(int) * m->chunks.size());
+        if (e == cudaSuccess) e = cudaMemset(m->mode[b], 0, sizeof(int) * m->chunks.size());
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 static int alloc_mixed(MixedState* m, char* err, size_t len) {
     const size_t cells = (size_t)m->plane * 3;
     for (int b = 0; b < 2; b++) {
@@ -983,6 +1209,10 @@ static int alloc_mixed(MixedState* m, char* err, size_t len) {
         snprintf(err, len, "cudaMalloc of item flags failed");
         return SHLL_ERR_NOMEM;
     }
+    if (alloc_mode_flags(m) != cudaSuccess) {
+        snprintf(err, len, "cudaMalloc of the pair-flux flags failed");
+        return SHLL_ERR_NOMEM;
+    }
     if (cudaMalloc(&m->d_tubes, sizeof(TubeP) * m->nitems) != cudaSuccess ||
         cudaMalloc(&m->d_flag, sizeof(int)) != cudaSuccess || cudaMemset(m->d_flag, 0, sizeof(int)) != cudaSuccess) {
         snprintf(err, len, "cudaMalloc of descriptors failed");
@@ -1018,6 +1248,12 @@ static TubeP tube_params(const shll_params& p, long base) {
     tp.Rf = (float)tp.R;
     tp.cvinvf = (float)(1.0 / tp.CV);
     tp.alpha = (float)p.mc_alpha;
+    const double pairs[2] = {tp.gamma * tp.RoCV, tp.RoCV};
+    float* outs[2] = {tp.gg1p, tp.gm1p};
+    for (int q = 0; q < 2; q++) {
+        outs[q][0] = (float)pairs[q];
+        outs[q][1] = (float)(pairs[q] - (double)outs[q][0]);
+    }
     int ex;
     tp.lam_pow2 = std::frexp(tp.lam, &ex) == 0.5 && ex > -100 && ex < 100;
     tp.steps = 0;
@@ -1106,6 +1342,8 @@ void mixed_destroy(MixedState* m) {
         cudaFree(m->dh[b]); cudaFree(m->dl[b]);
     }
     cudaFree(m->frames);
+    cudaFree(m->mode[0]);
+    cudaFree(m->mode[1]);
     cudaFree(m->prog);
     cudaFree(m->stage);
     cudaFree(m->d_bad);
@@ -1412,6 +1650,8 @@ static std::atomic<int> g_resident{1};
 extern "C" void shll_set_resident(int on) { g_resident = on ? 1 : 0; }
 static std::atomic<int> g_stall{-1};
 extern "C" void shll_debug_stall_chunk(int chunk) { g_stall = chunk; }
+static std::atomic<int> g_pair_flux{1};
+extern "C" void shll_set_pair_flux(int on) { g_pair_flux = on == 2 ? 2 : (on ? 1 : 0); }
 
 // issues the launches of one run on m->stream: the sweeps of every variant group (or, resident,
 // one launch for all sweeps of the run's single variant group), then the fix-up
@@ -1442,7 +1682,17 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
     A.item_flags = m->d_item_flags;
     A.stall_id = resident ? g_stall.load() : -1;
     A.sweep = 0;
-    long n = 0;
+    const bool pairs = g_pair_flux.load() && m->mode[0];
+    A.mode[0] = pairs ? m->mode[0] : nullptr;
+    A.mode[1] = pairs ? m->mode[1] : nullptr;
+    A.pair_m2 = g_pair_flux.load() == 2 ? -1.0f : kPairMach * kPairMach;
+    long n = 0, extra = 0;
+    if (pairs) {  // the flags of the state at the start of the run
+        A.chunk0 = 0;
+        if (m->kahan) k_mode1d<true><<<(unsigned)order.size(), 256, 0, m->stream>>>(A);
+        else k_mode1d<false><<<(unsigned)order.size(), 256, 0, m->stream>>>(A);
+        extra++;
+    }
     if (resident) {
         A.chunk0 = 0;
         cudaError_t e = cudaMemsetAsync(m->prog, 0, sizeof(unsigned) * kProgStride * order.size(), m->stream);
@@ -1458,16 +1708,21 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
             const int cnt = g.active[k + 1];
             if (cnt == 0) continue;
             A.chunk0 = g.first;
-            const cudaError_t e = launch_sweep(g.variant, m->kahan, cnt, m->stream, A, n > 0);
+            cudaError_t e = launch_sweep(g.variant, m->kahan, cnt, m->stream, A, n > 0);
             if (e != cudaSuccess) return e;
             n++;
+            if (pairs && g.variant <= 1) {  // first order: the same chunks' pair-flux form
+                e = launch_sweep_ff(g.variant, m->kahan, cnt, m->stream, A, true);
+                if (e != cudaSuccess) return e;
+                n++;
+            }
         }
     }
     A.chunk0 = 0;
     const int nch = (int)order.size();
     if (m->kahan) k_fixup1d<true><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);
     else k_fixup1d<false><<<(nch + 127) / 128, 128, 0, m->stream>>>(A, nch);
-    *launches = n + 1;
+    *launches = n + extra + 1;
     return cudaGetLastError();
 }
 
@@ -1606,6 +1861,7 @@ static int rebuild_chunks(MixedState* m, char* err, size_t len) {
         if (!m->dh[b])
             ok = cudaMalloc(&m->dh[b], cells * sizeof(float)) == cudaSuccess &&
                  cudaMalloc(&m->dl[b], cells * sizeof(float)) == cudaSuccess;
+    ok = ok && alloc_mode_flags(m) == cudaSuccess;
     if (!ok) { snprintf(err, len, "re-chunking allocation failed"); return SHLL_ERR_NOMEM; }
     return SHLL_OK;
 }
@@ -1878,8 +2134,10 @@ constexpr size_t kStaticChunkOff = kStaticBSumOff + 2 * kStaticMaxChunks * sizeo
 constexpr size_t kStaticTubeOff = (kStaticChunkOff + kStaticMaxChunks * sizeof(Chunk) + 255) / 256 * 256;
 constexpr size_t kStaticFlagOff = kStaticTubeOff + (sizeof(TubeP) + 255) / 256 * 256;
 static_assert(kStaticFlagOff >= kStaticTubeOff + sizeof(TubeP), "the tube descriptor overlaps the error flag");
+constexpr size_t kStaticModeOff = kStaticFlagOff + 256;                               // 2 x int[256]
 constexpr size_t kStaticScratchBytes = 2u << 20;
-static_assert(kStaticFlagOff + 256 <= kStaticScratchBytes, "static scratch layout exceeds its array");
+static_assert(kStaticModeOff + 2 * kStaticMaxChunks * sizeof(int) <= kStaticScratchBytes,
+              "static scratch layout exceeds its array");
 constexpr int kStaticMaxDevices = 64;
 }  // namespace
 
@@ -1995,11 +2253,23 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.item_flags = nullptr;
     A.stall_id = -1;
     A.chunk0 = 0;
+    // first order: the pair-flux flags, as in the context API (two ints per chunk in the array;
+    // the start-of-run kernel writes them before the first sweep reads them)
+    const bool pairs = tp.order == 1 && g_pair_flux.load();
+    A.mode[0] = pairs ? reinterpret_cast<int*>(sc + kStaticModeOff) : nullptr;
+    A.mode[1] = pairs ? A.mode[0] + kStaticMaxChunks : nullptr;
+    A.pair_m2 = g_pair_flux.load() == 2 ? -1.0f : kPairMach * kPairMach;
     const long nsweeps = (nsteps + B - 1) / B;
-    shll_count_launches(nsweeps + 1);
+    e = allow_solo_padding();
+    if (e == cudaSuccess && pairs) {
+        k_mode1d<false><<<k, 256, 0, s>>>(A);
+        e = cudaGetLastError();
+    }
+    shll_count_launches((pairs ? 2 * nsweeps + 1 : nsweeps) + 1);
     for (long w = 0; w < nsweeps && e == cudaSuccess; w++) {
         A.sweep = (int)w;
         e = launch_sweep(tube_variant(tp), false, k, s, A, w > 0);
+        if (e == cudaSuccess && pairs) e = launch_sweep_ff(tube_variant(tp), false, k, s, A, true);
     }
     if (e != cudaSuccess) {
         fprintf(stderr, "shll_tube_run_static: sweep launch failed: %s\n", cudaGetErrorString(e));

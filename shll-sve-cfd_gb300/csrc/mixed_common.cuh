@@ -257,3 +257,90 @@ __device__ __forceinline__ float d2f_bits(double x) {  // truncation to FP32 (sa
     d2ff_bits(x, h, l);
     return h;
 }
+
+// ---- double-FP32 ("float-float") arithmetic on packed FP32x2 lanes ----------------------------
+// A value is an unevaluated sum h + l of two FP32 numbers (about 48 significant bits).  Products
+// use the exact FMA residual (fma(a, b, -a*b) is the rounding error of a*b), sums the TwoSum
+// error-free transformation; the absolute error of a sum or product is about 2^-46 of its largest
+// operand.  Used by the first-order sweeps of chunks in supersonic flow, where the reference scheme
+// amplifies per-step rounding errors (its split gives the u - a wave the negative numerical
+// viscosity a(1 - M)/2 once M > 1), so that FP32 rounding is not enough there.
+struct FF2 {
+    float2 h, l;
+};
+__device__ __forceinline__ FF2 ffv(float h, float l) { return {f2(h), f2(l)}; }
+__device__ __forceinline__ FF2 ffneg(FF2 a) { return {neg2(a.h), neg2(a.l)}; }
+// a * s for a power of two s (exact)
+__device__ __forceinline__ FF2 ffscale(FF2 a, float s) { return {mul2(a.h, f2(s)), mul2(a.l, f2(s))}; }
+// renormalisation of p + e with |e| small against |p|
+__device__ __forceinline__ FF2 ffnorm(float2 p, float2 e) {
+    const float2 h = add2(p, e);
+    return {h, sub2(e, sub2(h, p))};
+}
+// sum without the final renormalisation: (s, e) with e = the rounding error of the high parts plus
+// the low parts; for sums that feed another sum or a product
+__device__ __forceinline__ FF2 ffadd_u(FF2 a, FF2 b) {
+    const float2 s = add2(a.h, b.h);
+    const float2 bp = sub2(s, a.h);
+    const float2 e = add2(sub2(a.h, sub2(s, bp)), sub2(b.h, bp));
+    return {s, add2(e, add2(a.l, b.l))};
+}
+__device__ __forceinline__ FF2 ffadd(FF2 a, FF2 b) {
+    const FF2 t = ffadd_u(a, b);
+    return ffnorm(t.h, t.l);
+}
+__device__ __forceinline__ FF2 ffsub(FF2 a, FF2 b) { return ffadd(a, ffneg(b)); }
+// product left unnormalised, (p, e) with |e| <= about 2^-22 |p|; for products that feed a sum or
+// another product, which renormalise
+__device__ __forceinline__ FF2 ffmul_u(FF2 a, FF2 b) {
+    const float2 p = mul2(a.h, b.h);
+    float2 e = fma2(a.h, b.h, neg2(p));
+    e = fma2(a.h, b.l, e);
+    return {p, fma2(a.l, b.h, e)};
+}
+__device__ __forceinline__ FF2 ffmul(FF2 a, FF2 b) {
+    const FF2 t = ffmul_u(a, b);
+    return ffnorm(t.h, t.l);
+}
+// 1/a: r0 = approximate FP32 reciprocal, e = 1 - a r0 (FMA residuals), r = r0 (1 + e + e^2)
+__device__ __forceinline__ FF2 ffrcp(FF2 a) {
+    const float2 r0 = rcp2(a.h);
+    float2 e = fma2(neg2(a.h), r0, f2(1.0f));
+    e = fma2(neg2(a.l), r0, e);
+    return ffnorm(r0, mul2(r0, fma2(e, e, e)));
+}
+// sqrt(a), a > 0: FP32 estimate s0 from a Newton-refined reciprocal square root y, then
+// s = s0 + (a - s0^2) y / 2 (the residual a - s0^2 from an FMA)
+__device__ __forceinline__ FF2 ffsqrt(FF2 a) {
+    float2 y = rsqrt2(a.h);
+    y = mul2(y, fma2(mul2(f2(-0.5f), a.h), mul2(y, y), f2(1.5f)));
+    const float2 s0 = mul2(a.h, y);
+    const float2 e = add2(fma2(neg2(s0), s0, a.h), a.l);
+    return ffnorm(s0, mul2(mul2(f2(0.5f), e), y));
+}
+
+// The split fluxes of two cells (FP32x2 lanes) with conserved state U (pairs), evaluated directly
+// in double-FP32 arithmetic (base-c/base_shll.c:134-158 with P = (gamma-1)(E - m u / 2), which
+// equals rho R T, and a^2 = gamma R T = gamma (gamma-1) (E - m u / 2) / rho).  Absolute errors are
+// about 2^-45 of the flux magnitudes, so no deviation form is needed.  gg1 = gamma (gamma-1),
+// gm1 = gamma - 1, as pairs.
+__device__ __forceinline__ void flux1x2_ff(const FF2 U[3], FF2 gg1, FF2 gm1, FF2 fp[3], FF2 fm[3]) {
+    const FF2 r = ffrcp(U[0]);
+    const FF2 u = ffmul(U[1], r);
+    const FF2 mu = ffmul_u(U[1], u);
+    const FF2 eint = ffsub(U[2], ffscale(mu, 0.5f));
+    const FF2 P = ffmul(gm1, eint);
+    const FF2 a = ffsqrt(ffmul(gg1, ffmul_u(eint, r)));
+    const FF2 M = ffmul(u, ffrcp(a));
+    const FF2 Z1 = ffscale(ffadd(M, ffv(1.0f, 0.0f)), 0.5f);
+    const FF2 Z2 = ffmul(ffscale(a, 0.5f), ffsub(ffv(1.0f, 0.0f), ffmul_u(M, M)));
+    FF2 F[3];
+    F[0] = U[1];
+    F[1] = ffadd(mu, P);
+    F[2] = ffmul(u, ffadd_u(U[2], P));
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        fp[k] = ffadd(ffmul_u(F[k], Z1), ffmul_u(U[k], Z2));
+        fm[k] = ffsub(F[k], fp[k]);
+    }
+}

@@ -1,9 +1,10 @@
-// Plain FP64 batches (SHLL_PREC_F64 items of shll_batch_*): many independent tubes or domains,
-// one launch per time step (per order) over the blocks of every item that still has steps.
-// The per-block arithmetic is the plain single-problem kernel's (shll_plain.cuh), i.e. the
-// reference's FP64 arithmetic with fused multiply-add allowed.
+// Plain FP64 batches (SHLL_PREC_F64 or SHLL_PREC_F64_EXACT items of shll_batch_*): many
+// independent tubes or domains, one launch per time step (per order) over the blocks of every
+// item that still has steps.  The per-block arithmetic is the plain single-problem kernel's
+// (shll_plain.cuh): the reference's FP64 arithmetic with fused multiply-add allowed (the kernels
+// of this unit), or without it, bit-identical to the FP64 reference build (plain_batch_exact.cu).
 #define SHLL_PLAIN_NS plain_batch_ns
-#include "shll_plain.cuh"
+#include "plain_batch_kernels.cuh"
 
 #include <algorithm>
 #include <cstdio>
@@ -12,48 +13,17 @@
 
 #include "plain_batch.h"
 
-namespace plain_batch_ns {
 
-struct PItem {
-    long base;        // cell offset in the planes
-    int nx, ny;       // ny = 1 in 1D
-    int order, steps, par;
-    Gas<double> g;
-};
-
-struct PBlk { int item, a, b; };  // 1D: first cell a; 2D: tile origin (a, b) = (i0, j0)
-
-// (flag points at the item's own flag word; the kernel ORs SHLL_FLAG_NONPOSITIVE into it)
-template <int ORDER>
-__global__ void __launch_bounds__(T1) k_batch1(const PItem* __restrict__ items, const PBlk* __restrict__ blks,
-                                               double* U0, double* U1, long plane, int step, int* flags) {
-    const PBlk bk = blks[blockIdx.x];
-    const PItem it = items[bk.item];
-    if (step >= it.steps) return;
-    const int inb = (it.par + step) & 1;
-    const double* Uin = (inb ? U1 : U0) + it.base;
-    double* Uout = (inb ? U0 : U1) + it.base;
-    step1_block<double, ORDER>(Uin, Uout, it.nx, plane, it.g, flags + bk.item, bk.a);
-}
-
-template <int ORDER>
-__global__ void __launch_bounds__(TI * TJ) k_batch2(const PItem* __restrict__ items, const PBlk* __restrict__ blks,
-                                                    double* U0, double* U1, long plane, int step, int* flags) {
-    const PBlk bk = blks[blockIdx.x];
-    const PItem it = items[bk.item];
-    if (step >= it.steps) return;
-    const int inb = (it.par + step) & 1;
-    const double* Uin = (inb ? U1 : U0) + it.base;
-    double* Uout = (inb ? U0 : U1) + it.base;
-    step2_tile<double, ORDER>(Uin, Uout, it.nx, it.ny, plane, it.g, flags + bk.item, bk.a, bk.b);
-}
-
-}  // namespace plain_batch_ns
 
 using namespace plain_batch_ns;
 
+// the kernels of plain_batch_exact.cu (the same item and block layouts, from the same header)
+cudaError_t plain_batch_exact_launch(int dim, int order, int nb, cudaStream_t s, const void* items, const void* blks,
+                                     double* U0, double* U1, long plane, int step, int* flags);
+
 struct PlainBatch {
     int dim = 1, count = 0, nv = 3;
+    bool exact = false;        // SHLL_PREC_F64_EXACT items
     cudaStream_t stream = nullptr;
     std::vector<shll_params> params;
     std::vector<PItem> items;
@@ -73,11 +43,14 @@ PlainBatch* plain_batch_create(const shll_params* p, int count, cudaStream_t s, 
     b->dim = p[0].dim;
     b->nv = b->dim == 2 ? 4 : 3;
     b->params.assign(p, p + count);
+    b->exact = p[0].precision == SHLL_PREC_F64_EXACT;
     long off = 0;
     for (int t = 0; t < count; t++) {
         const shll_params& q = p[t];
-        if (q.dim != b->dim || q.precision != SHLL_PREC_F64) {
-            snprintf(err, len, "plain batches take SHLL_PREC_F64 items of one dimension");
+        if (q.dim != b->dim || q.precision != p[0].precision ||
+            (q.precision != SHLL_PREC_F64 && q.precision != SHLL_PREC_F64_EXACT)) {
+            snprintf(err, len, "plain batches take SHLL_PREC_F64 or SHLL_PREC_F64_EXACT items of one dimension and "
+                               "one precision");
             delete b;
             return nullptr;
         }
@@ -199,28 +172,21 @@ int plain_batch_run(PlainBatch* b, char* err, size_t len) {
         snprintf(err, len, "plain batch: item upload failed");
         return SHLL_ERR_CUDA;
     }
-    if (b->dim == 2) {
-        cudaFuncSetAttribute(k_batch2<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2<double, 1>());
-        cudaFuncSetAttribute(k_batch2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2<double, 2>());
-    }
     long launches = 0;
-    for (long s = 0; s < maxsteps; s++) {
-        for (int o = 0; o < 2; o++) {
+    cudaError_t e = cudaSuccess;
+    for (long s = 0; s < maxsteps && e == cudaSuccess; s++) {
+        for (int o = 0; o < 2 && e == cudaSuccess; o++) {
             const int nb = active[o][s + 1];
             if (nb == 0) continue;
             launches++;
-            if (b->dim == 1) {
-                if (o == 0) k_batch1<1><<<nb, T1, 0, b->stream>>>(b->d_items, b->d_blk[0], b->U[0], b->U[1], b->plane, (int)s, b->d_flag);
-                else k_batch1<2><<<nb, T1, 0, b->stream>>>(b->d_items, b->d_blk[1], b->U[0], b->U[1], b->plane, (int)s, b->d_flag);
-            } else {
-                dim3 blk(TJ, TI);
-                if (o == 0) k_batch2<1><<<nb, blk, smem2<double, 1>(), b->stream>>>(b->d_items, b->d_blk[0], b->U[0], b->U[1], b->plane, (int)s, b->d_flag);
-                else k_batch2<2><<<nb, blk, smem2<double, 2>(), b->stream>>>(b->d_items, b->d_blk[1], b->U[0], b->U[1], b->plane, (int)s, b->d_flag);
-            }
+            e = b->exact ? plain_batch_exact_launch(b->dim, o + 1, nb, b->stream, b->d_items, b->d_blk[o], b->U[0],
+                                                    b->U[1], b->plane, (int)s, b->d_flag)
+                         : batch_launch(b->dim, o + 1, nb, b->stream, b->d_items, b->d_blk[o], b->U[0], b->U[1],
+                                        b->plane, (int)s, b->d_flag);
         }
     }
     shll_count_launches(launches);
-    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { snprintf(err, len, "plain batch launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     for (int t = 0; t < b->count; t++) {
         b->par[t] = (b->par[t] + b->items[t].steps) & 1;

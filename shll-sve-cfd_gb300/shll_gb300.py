@@ -58,7 +58,7 @@ EXPORTS = [
     "shll_batch_set_stream", "shll_batch_item_status", "shll_set_graph_replay", "shll_batch_checkpoint",
     "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
     "shll_set_resident", "shll_debug_stall_chunk", "shll_batch_set_primitives", "shll_initial_primitives",
-    "shll_batch_set_all_primitives", "shll_batch_get_all_primitives",
+    "shll_batch_set_all_primitives", "shll_batch_get_all_primitives", "shll_set_pair_flux",
 ]
 
 
@@ -176,6 +176,12 @@ def set_graph_replay(on):
 def set_resident(on):
     """Run single-wave mixed-precision 1D runs as one resident launch (default on)."""
     lib().shll_set_resident(1 if on else 0)
+
+
+def set_pair_flux(on):
+    """Evaluate first-order fluxes in double-FP32 arithmetic where the flow is supersonic (default 1; 0 off,
+    2 in every first-order chunk)."""
+    lib().shll_set_pair_flux(int(on))
 
 
 def debug_stall_chunk(chunk):
