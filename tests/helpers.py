@@ -26,3 +26,26 @@ def max_rel_scaled(a, b):
 
 def l1(a, b):
     return np.mean(np.abs(np.asarray(a) - np.asarray(b)), axis=-1)
+
+
+def batch1d_draws(count=4096, seed=0):
+    """The seeded batch of independent 1D shock tubes (4096 tubes, seed 0): per tube, in this draw
+    order, cells round(exp(U(ln 256, ln 16384))), density ratio U(2, 100), temperature ratio
+    U(0.5, 2), diaphragm position U(0.3, 0.7); first order for the first half, second order after.
+    Returns (index, cells, density ratio, temperature ratio, diaphragm, order) tuples."""
+    import math
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(256), math.log(16384)))))
+        ratio = float(rng.uniform(2, 100))
+        tr = float(rng.uniform(0.5, 2))
+        xd = float(rng.uniform(0.3, 0.7))
+        out.append((t, n, ratio, tr, xd, 1 if t < count // 2 else 2))
+    return out
+
+
+def tube_params(shll, draw, precision):
+    t, n, ratio, tr, xd, order = draw
+    return shll.params(1, order, nx=n, precision=precision, t_end=0.2, ic_x_d=xd, ic_rho_l=ratio, ic_T_l=tr,
+                       ic_rho_r=1.0, ic_T_r=1.0, ic_u_l=0.0, ic_u_r=0.0)
