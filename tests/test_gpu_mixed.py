@@ -5,11 +5,14 @@ Tolerances: L1(rho, u, T) <= 1e-6 against the FP64 oracle for first-order tubes 
 tested and for second-order tubes up to 1024 cells; mass (and energy, with reflective walls)
 conserved to <= 1e-12 relative.  Second-order runs on long tubes amplify any rounding difference
 (even FP64 with and without fused multiply-add differ by L1(rho) ~ 8e-7 at 65536 cells), so
-larger second-order cases are checked against the exact Riemann solution instead."""
+larger second-order cases are checked against a small multiple of the scheme's own spread under
+FP32-scale perturbations (oracle/noise_floor.py), or against the exact Riemann solution within
+10 % of the FP64 run's distance to it."""
 import numpy as np
 import pytest
 
 from helpers import l1
+from noise_floor import spread_stepwise
 
 pytestmark = pytest.mark.gpu
 
@@ -62,11 +65,25 @@ def test_partial_steps_then_run(shll, oracle):
     assert np.all(l1(ctx.primitives(), ref) <= 1e-6)
 
 
+def fp64_sod(shll, n, order=2):
+    # the bit-exact FP64 path (the oracle's arithmetic) on the Sod tube
+    c = shll.Context(shll.params(1, order, nx=n, precision="f64_exact"))
+    c.init_state()
+    c.run()
+    out = c.primitives()
+    c.close()
+    return out
+
+
 def test_second_order_large_tube_vs_exact_riemann(shll, oracle):
+    # second order is chaotic at this size (oracle/noise_floor.py), so the check is physical: the
+    # mixed run's distance to the exact Riemann solution within 10 % of the FP64 run's
     n = 8192
     s, out, t0, t1 = run_mixed(shll, shll.params(1, 2, nx=n, precision="mixed_f64"))
     ex = oracle.riemann_exact(n, s * (0.125 / n))
-    assert np.mean(np.abs(out[0] - ex[0])) < 0.003
+    e_mixed = np.mean(np.abs(out[0] - ex[0]))
+    e_fp64 = np.mean(np.abs(fp64_sod(shll, n)[0] - ex[0]))
+    assert abs(e_mixed - e_fp64) <= 0.1 * e_fp64, (e_mixed, e_fp64)
     assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
 
 
@@ -85,7 +102,11 @@ def test_batch_matches_single_contexts_and_oracle(shll, oracle):
     b.run()
     for i, p in enumerate(items):
         out = b.primitives(i)
-        tol = 1e-6 if (p.order == 1 or p.nx <= 1024) else 1e-4
+        # second order beyond 1024 cells: within twice the scheme's own spread under FP32-scale
+        # perturbations repeated every 10 steps (oracle/noise_floor.py), or 1e-6
+        tol = 1e-6
+        if p.order == 2 and p.nx > 1024:
+            tol = max(1e-6, 2 * float(np.max(spread_stepwise(p.nx, 2, p.ic.x_d, p.ic.rho_l, p.ic.T_l))))
         assert np.all(l1(out, refs[i]) <= tol), (i, p.nx, p.order, l1(out, refs[i]))
         single = shll.Context(p)
         single.init_state()
