@@ -49,3 +49,21 @@ def tube_params(shll, draw, precision):
     t, n, ratio, tr, xd, order = draw
     return shll.params(1, order, nx=n, precision=precision, t_end=0.2, ic_x_d=xd, ic_rho_l=ratio, ic_T_l=tr,
                        ic_rho_r=1.0, ic_T_r=1.0, ic_u_l=0.0, ic_u_r=0.0)
+
+
+def batch2d_draws(count=256, seed=1):
+    """The seeded batch of independent 2D first-order domains (256 domains, seed 1): per domain, in
+    this draw order, side uniform in {128, 256, 512, 1024}, diaphragm radius U(0.1, 0.35), inside /
+    outside density ratio U(2, 50), temperature ratio U(0.5, 2); gas at rest, 400 steps.
+    Returns (index, side, radius, density ratio, temperature ratio) tuples."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in range(count):
+        n = int(rng.choice([128, 256, 512, 1024]))
+        out.append((t, n, float(rng.uniform(0.1, 0.35)), float(rng.uniform(2, 50)), float(rng.uniform(0.5, 2))))
+    return out
+
+
+def circle_params(shll, n, radius, ratio, tr, steps, precision):
+    return shll.params(2, 1, nx=n, ny=n, precision=precision, n_steps=steps, ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5,
+                       ic_cy=0.5, ic_radius=radius, ic_rho_l=ratio, ic_T_l=tr, ic_rho_r=1.0, ic_T_r=1.0)
