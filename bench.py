@@ -282,6 +282,11 @@ class Problem:
             return []
         return [i for i in range(len(self.items)) if self.obj.item_status(i) != 0]
 
+    def close(self):
+        if self.obj is not None:
+            self.obj.close()
+            self.obj = None
+
     def result(self):
         if self.batch:
             return [self.obj.primitives(i) for i in range(len(self.items))]
@@ -399,6 +404,91 @@ def job_value(world, cell_updates_per_run, runs, seconds):
     return world * cell_updates_per_run * runs / seconds
 
 
+DEFAULT_CELLS = {"sod1d": 65536, "circle2d": 4096}
+
+
+def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, world, rank, local, extras):
+    """One workload on this rank's GPU: W untimed runs, then `steps` timed runs (CUDA events on the
+    launching stream, L2 flushed before each), the end-to-end leg through the public API with host
+    buffers, and (rank 0, extras) the FP64 comparison and the CPU baseline.  Returns the JSON fields."""
+    prob = Problem(shll, workload, args.precision, cells, order, args.fold, stream, tune=not args.no_tune)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    for _ in range(W):
+        prob.reset()
+        prob.run()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = 0
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(steps):
+            prob.reset()
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+            torch.cuda.synchronize()
+            la = shll.kernel_launches()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prob.run()
+            e1.record(stream)
+            e1.synchronize()
+            launches += shll.kernel_launches() - la
+            times.append(e0.elapsed_time(e1) / 1000.0)
+    torch.cuda.synchronize()
+    t_total = max_over_ranks(sum(times), dist, "cuda")
+    value = job_value(world, prob.cu, steps, t_total)
+    mixed_out = prob.result()
+
+    # roofline: algorithmic bytes (48 per 1D, 64 per 2D cell-update) of the timed runs over their
+    # CUDA-event time, i.e. per launch of the run's kernels over their average launch duration
+    hbm, peak_kind = peaks()
+    bytes_per_cu = 64.0 if prob.dim == 2 else 48.0
+    kernel = {"sod1d": "k_tube1d" if launches <= 3 * steps else "k_sweep1d", "batch1d": "k_sweep1d",
+              "circle2d": "k_step2d", "batch2d": "k_step2d"}[workload]
+    achieved = bytes_per_cu * prob.cu * steps / t_total / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": profile_traffic(kernel, workload), "peak_kind": peak_kind, "kernel": kernel,
+                "algorithmic_bytes_per_run": bytes_per_cu * prob.cu, "launches_per_run": launches / steps,
+                "launch_duration_s": t_total / max(1, launches),
+                "note": "algorithmic bytes of the timed runs / their CUDA-event time (effective: the state is "
+                        "read and written once per fold window)"}
+
+    # end to end through the C-ABI with host buffers: every step uploads every item's initial
+    # primitives from pinned host memory, runs, and downloads the result primitives
+    host_in, host_out = prob.host_buffers(torch)
+    e_times = []
+    for _ in range(max(1, min(steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prob.upload(host_in)
+        prob.run()
+        prob.download(host_out)
+        torch.cuda.synchronize()
+        e_times.append(time.perf_counter() - t0)
+    e2e_identical = all(np.array_equal(a, b, equal_nan=True)
+                        for a, b in zip(host_out, mixed_out if prob.batch else [mixed_out]))
+    h2d = d2h = sum(b.nbytes for b in host_in)
+    e2e_value = world * prob.cu * len(e_times) / sum(e_times)
+    out = {
+        "value": value, "unit": "cell-updates/s", "steps": steps, "warmup": W, "ms_per_step": 1000 * t_total / steps,
+        "config": {"workload": describe(workload, cells, order), "name": workload, "cells": cells or None,
+                   "order": order if workload == "sod1d" else None, "cell_updates_per_run": prob.cu,
+                   "precision": args.precision, "fold_steps": args.fold or ("autotuned" if prob.tuning() else 64),
+                   "tuning": prob.tuning(), "parallelism": f"replicas{world}",
+                   "l2": "flushed between runs (256 MB write)"},
+        "roofline": roofline,
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "host_memory": "pinned", "result_identical_to_device_run": e2e_identical},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if extras and rank == 0:
+        out.update(fp64_comparison(shll, torch, stream, prob, args, cells, order, mixed_out, t_total / steps))
+    prob.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -412,21 +502,24 @@ def main():
     ap.add_argument("--precision", default="mixed_f64")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison runs and CPU baseline")
     ap.add_argument("--no-tune", action="store_true", help="1D mixed: skip the autotuner (library defaults)")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="measure only --workload (by default the sod1d line also carries batch1d, circle2d "
+                         "and batch2d under 'workloads')")
+    ap.add_argument("--other-steps", type=int, default=3, help="timed runs of each other workload")
     args = ap.parse_args()
     workload = args.workload
     if args.cells == 0:
-        args.cells = {"sod1d": 65536, "circle2d": 4096}.get(workload, 0)
+        args.cells = DEFAULT_CELLS.get(workload, 0)
     W = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    desc = describe(workload, args.cells, args.order)
-    config = {"workload": desc, "name": workload, "cells": args.cells or None,
-              "order": args.order if workload == "sod1d" else None}
 
     if args.impl == "reference":
         if rank != 0:
             return
+        config = {"workload": describe(workload, args.cells, args.order), "name": workload,
+                  "cells": args.cells or None, "order": args.order if workload == "sod1d" else None}
         value, ms, sample, cores = reference_arm(args, workload, args.warmup)
         print(json.dumps({
             "impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
@@ -446,103 +539,32 @@ def main():
         dist.init_process_group("nccl")
     shll = load_pkg()
     stream = torch.cuda.Stream()
-    prob = Problem(shll, workload, args.precision, args.cells, args.order, args.fold, stream, tune=not args.no_tune)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
-    for _ in range(W):
-        prob.reset()
-        prob.run()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    l0 = shll.kernel_launches()
-    launches = 0
-    times = []
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            prob.reset()
-            with torch.cuda.stream(stream):
-                flush.add_(1.0)
-            torch.cuda.synchronize()
-            la = shll.kernel_launches()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            prob.run()
-            e1.record(stream)
-            e1.synchronize()
-            launches += shll.kernel_launches() - la
-            times.append(e0.elapsed_time(e1) / 1000.0)
-    torch.cuda.synchronize()
-    t_total = max_over_ranks(sum(times), dist, "cuda")
-    value = job_value(world, prob.cu, args.steps, t_total)
-    ms_per_step = 1000 * t_total / args.steps
-    mixed_out = prob.result()
-
-    # roofline of the dominant kernel: algorithmic bytes / (timed region / its launches)
-    hbm, peak_kind = peaks()
-    bytes_per_cu = 64.0 if prob.dim == 2 else 48.0
-    # 1D runs that fit on the GPU at once are one resident launch (k_tube1d) plus the fix-up;
-    # larger ones one k_sweep1d launch per sweep
-    kernel = "k_step2d" if prob.dim == 2 else ("k_tube1d" if launches == 2 * args.steps else "k_sweep1d")
-    main_launches = max(1, launches - args.steps)  # minus the one fix-up launch per run
-    avg_launch = t_total / main_launches
-    bytes_per_launch = bytes_per_cu * prob.cu * args.steps / main_launches
-    achieved = bytes_per_launch / avg_launch / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": profile_traffic(kernel, workload), "peak_kind": peak_kind, "kernel": kernel,
-                "algorithmic_bytes_per_launch": bytes_per_launch, "launch_duration_s": avg_launch,
-                "note": "launch duration = CUDA-event time of the timed runs / launches (includes gaps)"}
-
-    # end to end through the C-ABI with host buffers: upload the initial state, run, download
-    # (every step: the initial primitives of every item from pinned host memory through
-    # set_primitives, the run, the result primitives back into pinned host memory)
-    host_in, host_out = prob.host_buffers(torch)
-    e_times = []
-    for _ in range(max(1, min(args.steps, 3))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        prob.upload(host_in)
-        prob.run()
-        prob.download(host_out)
-        torch.cuda.synchronize()
-        e_times.append(time.perf_counter() - t0)
-    # the end-to-end result is the device-timed run's, bit for bit
-    e2e_identical = all(np.array_equal(a, b, equal_nan=True)
-                        for a, b in zip(host_out, mixed_out if prob.batch else [mixed_out]))
-    h2d = d2h = sum(b.nbytes for b in host_in)
-    e2e_value = world * prob.cu * len(e_times) / sum(e_times)
-
-    extras = {}
-    if not args.no_extras and rank == 0:
-        extras = fp64_comparison(shll, torch, stream, prob, args, mixed_out, t_total)
+    head = measure(shll, torch, stream, workload, args.cells, args.order, args, args.steps, W, dist, world, rank,
+                   local, not args.no_extras)
+    others = {}
+    if workload == "sod1d" and not args.no_other_workloads:
+        for w in ("batch1d", "circle2d", "batch2d"):
+            others[w] = measure(shll, torch, stream, w, DEFAULT_CELLS.get(w, 0), 1, args, args.other_steps, 3, dist,
+                                world, rank, local, not args.no_extras)
     if rank == 0:
-        line = {
-            "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
-            "steps": args.steps, "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64"
-            else args.precision, "data": "synthetic",
-            "config": dict(config, cell_updates_per_run=prob.cu, precision=args.precision,
-                           fold_steps=args.fold or ("autotuned" if prob.tuning() else 64),
-                           tuning=prob.tuning(),
-                           parallelism=f"replicas{world}",
-                           l2="flushed between runs (256 MB write)"),
-            "roofline": roofline,
-            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "host_memory": "pinned",
-                    "result_identical_to_device_run": e2e_identical},
-            "gpu_launches": launches,
-            "clocks": clk.summary(),
-        }
-        line.update(extras)
+        line = {"metric": "cell-updates/s", "value": head.pop("value"), "unit": head.pop("unit"), "n_gpus": world,
+                "steps": head.pop("steps"), "warmup": head.pop("warmup"), "ms_per_step": head.pop("ms_per_step"),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64" else args.precision,
+                "data": "synthetic"}
+        line.update(head)
+        if others:
+            line["workloads"] = others
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
 
 
-def cpu_baseline(workload, args):
+def cpu_baseline(workload, cells, order):
     """The CPU port of the reference timed on a bounded sample of the workload, 1 thread."""
     if workload in ("sod1d", "batch1d"):
-        n = args.cells if workload == "sod1d" else 4096
-        order = args.order if workload == "sod1d" else 2
+        n = cells if workload == "sod1d" else 4096
+        order = order if workload == "sod1d" else 2
         steps = max(50, int(3.0e8 / n))
         v, dt = cpu_sample(n, order, steps, 32)
         sample = f"{n} cells x {steps} time steps ({'order ' + str(order)}), FP32 as published, {dt:.1f} s"
@@ -554,7 +576,16 @@ def cpu_baseline(workload, args):
     return {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port", "sample": sample}
 
 
-def fp64_comparison(shll, torch, stream, prob, args, mixed_out, t_mixed):
+def batch_results(shll, stream, items):
+    b = shll.Batch(items)
+    b.set_stream(stream.cuda_stream)
+    b.run(allow_numeric=True)
+    out = [(b.primitives(i), b.item_status(i)) for i in range(len(items))]
+    b.close()
+    return out
+
+
+def fp64_comparison(shll, torch, stream, prob, args, cells, order, mixed_out, t_run):
     """Plain FP64 path (one launch per step) on the same workload (or a seeded subsample for the
     batches): throughput, L1 of the mixed result against it, CPU baseline."""
     out = {}
@@ -572,37 +603,58 @@ def fp64_comparison(shll, torch, stream, prob, args, mixed_out, t_mixed):
         e1.record(stream)
         e1.synchronize()
         t64 = e0.elapsed_time(e1) / 1000.0
-        cu64 = sum(p.nx * (p.ny if p.dim == 2 else 1) * shll.steps_for(p) for p in items64)
-        l1 = np.zeros(4 if prob.dim == 2 else 3)
-        worst = 0.0
-        failed_mixed = set(prob.failed())
-        fail64 = [idx[j] for j in range(len(idx)) if b.item_status(j) != 0]
-        ok = [(j, i) for j, i in enumerate(idx) if i not in failed_mixed and i not in fail64]
-        by_order = {}
-        for j, i in ok:
-            e = np.mean(np.abs(mixed_out[i] - b.primitives(j)), axis=1)
-            l1 += e / max(1, len(ok))
-            worst = max(worst, float(e[0]))
-            by_order.setdefault(prob.items[i].order, []).append(float(e[0]))
-        out["l1_rho_vs_fp64_by_order"] = {f"order{o}": {"items": len(v), "mean": float(np.mean(v)),
-                                                        "median": float(np.median(v)), "max": float(np.max(v)),
-                                                        "items_at_or_below_1e-6": int(sum(x <= 1e-6 for x in v))}
-                                          for o, v in sorted(by_order.items())}
+        fused = [(b.primitives(j), b.item_status(j)) for j in range(len(items64))]
         b.close()
-        out["items_broken_down"] = {"mixed_all_items": len(failed_mixed),
-                                    "fp64_sampled_items": len(fail64),
+        # the bit-exact FP64 path (the oracle's arithmetic): the reference of the L1 figures; the
+        # plain path's distance to it (fused multiply-add the only difference) measures how far the
+        # FP64 result of an item is reproducible at all
+        exact = batch_results(shll, stream, gen(shll, "f64_exact")[::sub])
+        cu64 = sum(p.nx * (p.ny if p.dim == 2 else 1) * shll.steps_for(p) for p in items64)
+        failed_mixed = set(prob.failed())
+        names = ["rho", "u", "v", "T"] if prob.dim == 2 else ["rho", "u", "T"]
+        by_order, l1s, worst, fail64 = {}, [], 0.0, 0
+        for j, i in enumerate(idx):
+            (pe, se), (pf, sf) = exact[j], fused[j]
+            if se != 0 or sf != 0:
+                fail64 += 1
+                continue
+            if i in failed_mixed:
+                by_order.setdefault(prob.items[i].order, []).append((np.inf, 0.0))
+                continue
+            e = np.mean(np.abs(mixed_out[i] - pe), axis=1)
+            floor = float(np.max(np.mean(np.abs(pf - pe), axis=1)))
+            l1s.append(e)
+            worst = max(worst, float(e[0]))
+            by_order.setdefault(prob.items[i].order, []).append((float(np.max(e)), floor))
+        summary = {}
+        for o, v in sorted(by_order.items()):
+            errs = np.array([x for x, _ in v])
+            rep = [x for x, f in v if f <= 1e-8]
+            other = [(x, f) for x, f in v if f > 1e-8]
+            summary[f"order{o}"] = {
+                "items": len(v), "median": float(np.median(errs)), "max": float(np.max(errs)),
+                "items_at_or_below_1e-6": int(np.sum(errs <= 1e-6)),
+                "fp64_reproducible_items": len(rep),
+                "fp64_reproducible_at_or_below_1e-6": int(sum(x <= 1e-6 for x in rep)),
+                "fp64_reproducible_max": float(max(rep)) if rep else None,
+                "others_max_ratio_to_fp64_floor": float(max(x / f for x, f in other)) if other else None}
+        out["l1_vs_fp64_by_order"] = summary
+        out["l1_note"] = ("max over rho, u, [v,] T of L1 against the bit-exact FP64 path on the sampled items; an "
+                          "item is FP64-reproducible when FP64 with and without fused multiply-add agree to 1e-8 "
+                          "(on the others the reference scheme amplifies rounding beyond that)")
+        out["items_broken_down"] = {"mixed_all_items": len(failed_mixed), "fp64_sampled_items": fail64,
                                     "mixed_sampled_items": len([i for i in idx if i in failed_mixed]),
                                     "note": "items whose density/energy went non-positive, overflowed or NaN "
                                             "(the reference scheme's own breakdown on strong tubes)"}
         out["fp64_plain"] = {"value": cu64 / t64, "unit": "cell-updates/s", "schedule": "one launch per step",
                              "precision": "f64", "sample": f"every {sub}th item ({len(items64)} items)"}
-        out["speedup_vs_fp64_plain"] = (prob.cu / (t_mixed / args.steps)) / (cu64 / t64)
-        names = ["rho", "u", "v", "T"] if prob.dim == 2 else ["rho", "u", "T"]
-        out["l1_vs_fp64"] = dict(zip(names, [float(x) for x in l1]), rho_worst_item=worst)
-        out["cpu_baseline"] = cpu_baseline(prob.workload, args)
+        out["speedup_vs_fp64_plain"] = (prob.cu / t_run) / (cu64 / t64)
+        if l1s:
+            out["l1_vs_fp64"] = dict(zip(names, [float(x) for x in np.mean(l1s, axis=0)]), rho_worst_item=worst)
+        out["cpu_baseline"] = cpu_baseline(prob.workload, cells, order)
         return out
     prec64 = "f64_exact" if prob.workload == "sod1d" else "f64"
-    p64 = params_single(shll, prob.workload, prec64, args.cells, args.order, 0)
+    p64 = params_single(shll, prob.workload, prec64, cells, order, 0)
     ctx = shll.Context(p64)
     ctx.set_stream(stream.cuda_stream)
     ctx.init_state()
@@ -619,15 +671,17 @@ def fp64_comparison(shll, torch, stream, prob, args, mixed_out, t_mixed):
     names = ["rho", "u", "v", "T"] if prob.dim == 2 else ["rho", "u", "T"]
     out["fp64_plain"] = {"value": prob.cu / t64, "unit": "cell-updates/s", "schedule": "one launch per step",
                          "precision": prec64}
-    out["speedup_vs_fp64_plain"] = (prob.cu / (t_mixed / args.steps)) / (prob.cu / t64)
+    out["speedup_vs_fp64_plain"] = (prob.cu / t_run) / (prob.cu / t64)
     out["l1_vs_fp64"] = dict(zip(names, [float(x) for x in l1]))
     if prob.workload == "sod1d":
         O = oracle_mod()
-        n = args.cells
-        ex = O.riemann_exact(n, shll.steps_for(prob.p) * (0.125 / n))
+        ex = O.riemann_exact(cells, shll.steps_for(prob.p) * (0.125 / cells))
         out["l1_rho_vs_exact_riemann"] = {"mixed": float(np.mean(np.abs(mixed_out[0] - ex[0]))),
                                           "fp64": float(np.mean(np.abs(f64_out[0] - ex[0])))}
-    out["cpu_baseline"] = cpu_baseline(prob.workload, args)
+        if order == 2:
+            out["l1_note"] = ("second order is chaotic at this size: the FP64 run from initial data perturbed by "
+                              "6e-8 relative moves by L1(rho) 5.05e-5 (oracle/noise_floor.py)")
+    out["cpu_baseline"] = cpu_baseline(prob.workload, cells, order)
     return out
 
 
