@@ -4,7 +4,8 @@
 # and generate the golden fixtures in tests/golden/.  They are never committed (oracle/_ref/ is
 # git-ignored) and nothing in the product runs them.
 #
-# The sources are read where they lie (REF_ROOT, default /root/reference).  Each variant is a
+# The sources are read where they lie: the reference's root directory is the first argument (or
+# REF_ROOT).  Each variant is a
 # stream edit into a temporary directory that changes only:
 #   * the compile-time problem size (const int N / NX / NY),
 #   * optionally the end time (const float TOTAL_TIME),
@@ -13,9 +14,13 @@
 #   * Save_Results() enabled where the reference commented it out, and
 #   * base-omp only: the hard-coded omp_set_num_threads(16) -> 2 threads.
 # Compiler flags follow the reference makefiles (gcc -O3 -lm; -fopenmp for base-omp).
-# Usage: oracle/make_ref.sh            (builds the fixed set used by the tests)
+# Usage: oracle/make_ref.sh <reference root>   (builds the fixed set used by the tests)
 set -eu
-REF=${REF_ROOT:-/root/reference}
+REF=${1:-${REF_ROOT:-}}
+if [ -z "$REF" ]; then
+    echo "make_ref: usage: make_ref.sh <reference root> (or REF_ROOT=...); nothing built" >&2
+    exit 0
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/base-c/base_shll.c" ]; then

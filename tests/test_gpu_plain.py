@@ -267,3 +267,26 @@ def test_batch_flags_the_items_that_break_down(shll, oracle, prec):
         got = b.primitives(i)
         err = max_rel_scaled(got, refs[i]) if prec == "f64" else np.max(np.mean(np.abs(got - refs[i]), axis=1))
         assert err <= tol, (i, err)
+
+
+def test_results_file_reads_like_the_reference_plot_script(shll):
+    # base-c/fetch_local.py: np.genfromtxt('./results.dat'), columns x y rho ux uy T, each reshaped
+    # to (NX, NY); a non-square grid so that a transposed layout would show
+    nx, ny = 40, 24
+    ctx = shll.Context(shll.params(2, 1, nx=nx, ny=ny, precision="mixed_f64", n_steps=30))
+    ctx.init_state()
+    ctx.run()
+    prim = ctx.primitives()
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "results.dat")
+        ctx.save_results(path)
+        data = np.genfromtxt(path)
+    ctx.close()
+    assert data.shape == (nx * ny, 6)
+    x_grid, y_grid, rho_grid = (data[:, k].reshape((nx, ny)) for k in (0, 1, 2))
+    T_grid = data[:, 5].reshape((nx, ny))
+    assert np.allclose(x_grid[:, 0], (np.arange(nx) + 0.5) / nx, rtol=1e-6)
+    assert np.all(x_grid == x_grid[:, :1]) and np.all(y_grid == y_grid[:1, :])
+    assert np.allclose(y_grid[0], (np.arange(ny) + 0.5) / ny, rtol=1e-6)
+    assert np.allclose(rho_grid, prim[0].reshape(nx, ny), rtol=1e-6)
+    assert np.allclose(T_grid, prim[3].reshape(nx, ny), rtol=1e-6)
