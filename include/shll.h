@@ -262,8 +262,10 @@ void shll_set_resident(int on);
  * exceeded Mach 0.6 at the end of a sweep (or, at the start of a run, held a pressure jump of more
  * than 1.5 times) evaluates its split fluxes, interface sums and increments of the next sweep in
  * double-FP32 arithmetic (pairs of FP32 numbers, about 48 significant bits) instead of FP32.
- * on = 0 keeps FP32 everywhere, on = 2 uses the pair flux in every chunk of every first-order
- * tube (default 1; process-wide). */
+ * on = 0 keeps FP32 everywhere; on = 2 uses the pair flux in every chunk of every tube, first
+ * and second order (the second-order scheme amplifies rounding everywhere, not only in supersonic
+ * flow: this is the mode in which second-order runs meet FP64 results to L1 1e-6 on long tubes,
+ * at about half the FP32 throughput) (default 1; process-wide). */
 void shll_set_pair_flux(int on);
 
 /* Test hook (no counterpart in the reference): in resident runs the chunk with this index (chunks

@@ -228,7 +228,6 @@ __device__ __forceinline__ T ldx(const T* p) {
 template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, bool RES, bool FF = false>
 __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch, const TubeP& tp, Smem1& S,
                             float2 (&dh)[3], float2 (&dl)[3], const bool reuse, const bool keep) {
-    static_assert(!FF || ORDER == 1, "the pair flux covers the first-order scheme");
     constexpr int R_ = ORDER;  // stencil reach per step
     Frame1& fr = S.fr;
 
@@ -264,7 +263,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
         asm volatile("griddepcontrol.wait;" ::: "memory");
         asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
         // (block-uniform: every thread reads the same flags)
-        if (ORDER == 1 && A.mode[0] && pair_mode(A, ch, sweep) != FF) return;
+        if (A.mode[0] && pair_mode(A, ch, sweep) != FF) return;
     }
     // (selects rather than indexing the parameter arrays, which would copy them to local memory)
     const void* hin = inb ? A.hi[1] : A.hi[0];
@@ -473,6 +472,10 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
             }
 #pragma unroll
             for (int k = 0; k < 3; k++) {
+                if (grx) {  // ghost fm_n of the right outflow wall (lane y holds no cell)
+                    fm[k].h.y = fm[k].h.x;
+                    fm[k].l.y = fm[k].l.x;
+                }
                 *reinterpret_cast<float2*>(&S.sfp[b][k][w0]) = fp[k].h;
                 *reinterpret_cast<float2*>(&S.sfm[b][k][w0]) = fm[k].h;
                 *at(sfpl, b, k, w0) = fp[k].l;
@@ -481,11 +484,38 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
             __syncthreads();
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                const float2 pLh = *reinterpret_cast<const float2*>(&S.sfp[b][k][jl]);  // fp_{w0-2}, fp_{w0-1}
-                const float2 mRh = *reinterpret_cast<const float2*>(&S.sfm[b][k][jr]);  // fm_{w0+2}, fm_{w0+3}
-                const float2 pLl = *at(sfpl, b, k, jl), mRl = *at(sfml, b, k, jr);
-                const FF2 IN = ffadd_u({make_float2(pLh.y, fp[k].h.x), make_float2(pLl.y, fp[k].l.x)}, fm[k]);
-                const FF2 OUT = ffadd_u(fp[k], {make_float2(fm[k].h.y, mRh.x), make_float2(fm[k].l.y, mRl.x)});
+                const FF2 pL = {*reinterpret_cast<const float2*>(&S.sfp[b][k][jl]), *at(sfpl, b, k, jl)};  // fp_{w0-2}, fp_{w0-1}
+                const FF2 mR = {*reinterpret_cast<const float2*>(&S.sfm[b][k][jr]), *at(sfml, b, k, jr)};  // fm_{w0+2}, fm_{w0+3}
+                FF2 IN, OUT;
+                if constexpr (ORDER == 1) {
+                    IN = ffadd_u({make_float2(pL.h.y, fp[k].h.x), make_float2(pL.l.y, fp[k].l.x)}, fm[k]);
+                    OUT = ffadd_u(fp[k], {make_float2(fm[k].h.y, mR.h.x), make_float2(fm[k].l.y, mR.l.x)});
+                } else {  // the FP32 step's reconstruction (see below), in pairs
+                    const FF2 pR = {*reinterpret_cast<const float2*>(&S.sfp[b][k][jr]), *at(sfpl, b, k, jr)};  // fp_{w0+2}
+                    const FF2 mL = {*reinterpret_cast<const float2*>(&S.sfm[b][k][jl]), *at(sfml, b, k, jl)};  // fm_{w0-1}
+                    // fp_{w0-1} (ghost of the left wall: fp_0) and fm_{w0+2} (ghost of the right wall: fm_{n-1})
+                    const float fplh = gl ? fp[k].h.x : pL.h.y, fpll = gl ? fp[k].l.x : pL.l.y;
+                    const float fmrh = gry ? fm[k].h.y : mR.h.x, fmrl = gry ? fm[k].l.y : mR.l.x;
+                    // differences f_j - f_{j-1}
+                    const FF2 dpo = ffsub(fp[k], {make_float2(fplh, fp[k].h.x), make_float2(fpll, fp[k].l.x)});  // j = w0, w0+1
+                    const FF2 dpr = ffsub({make_float2(fp[k].h.y, pR.h.x), make_float2(fp[k].l.y, pR.l.x)}, fp[k]);  // j = w0+1, w0+2
+                    const FF2 dmo = ffsub(fm[k], {make_float2(mL.h.y, fm[k].h.x), make_float2(mL.l.y, fm[k].l.x)});
+                    const FF2 dmr = ffsub({make_float2(fm[k].h.y, fmrh), make_float2(fm[k].l.y, fmrl)}, fm[k]);
+                    // lane x: fp_{w0-1} - fp_{w0-2}; lane y: fm_{w0+3} - fm_{w0+2}
+                    const FF2 dedge = ffsub({make_float2(fplh, mR.h.y), make_float2(fpll, mR.l.y)},
+                                            {make_float2(pL.h.x, fmrh), make_float2(pL.l.x, fmrl)});
+                    const FF2 sp = ffslope<LIM>(dpo, dpr, tp.alpha), sm = ffslope<LIM>(dmo, dmr, tp.alpha);
+                    // lane x: the slope of fp at w0-1; lane y: the slope of fm at w0+2
+                    const FF2 se = ffslope<LIM>({make_float2(dedge.h.x, dmr.h.y), make_float2(dedge.l.x, dmr.l.y)},
+                                                {make_float2(dpo.h.x, dedge.h.y), make_float2(dpo.l.x, dedge.l.y)}, tp.alpha);
+                    // reconstructed L_j = fp_j + sp_j/2 and R_j = fm_j - sm_j/2 (factors 0 on edge cells: exact)
+                    const FF2 Lo = ffadd(fp[k], {mul2(hp, sp.h), mul2(hp, sp.l)});
+                    const FF2 Ro = ffadd(fm[k], {mul2(nhm, sm.h), mul2(nhm, sm.l)});
+                    const float2 fe = make_float2(hpl, nhmr);
+                    const FF2 Le = ffadd({make_float2(fplh, fmrh), make_float2(fpll, fmrl)}, {mul2(fe, se.h), mul2(fe, se.l)});
+                    IN = ffadd_u({make_float2(Le.h.x, Lo.h.x), make_float2(Le.l.x, Lo.l.x)}, Ro);
+                    OUT = ffadd_u(Lo, {make_float2(Ro.h.y, Le.h.y), make_float2(Ro.l.y, Le.l.y)});
+                }
                 FF2 tin, tout;
                 if (LAM_POW2) {  // lam a power of two (or 0 where masked): exact scaling
                     tin = {mul2(lin2, IN.h), mul2(lin2, IN.l)};
@@ -673,16 +703,19 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
         const float eint = __fadd_rn(uf[2], -__fmul_rn(0.5f, __fdividef(__fmul_rn(uf[1], uf[1]), uf[0])));
         // breakdown: non-positive density or internal energy, or an overflowed / NaN increment
         bad |= !(uf[0] > 0.f) || !(eint > 0.f) || !finite;
-        // M^2 = m^2 / (rho^2 a^2) with a^2 = gamma (gamma-1) eint / rho
+        // M^2 = m^2 / (rho^2 a^2) with a^2 = gamma (gamma-1) eint / rho (second order: the pair flux
+        // only where it is asked for everywhere)
         if (ORDER == 1)
             fast |= __fmul_rn(uf[1], uf[1]) >
                     __fmul_rn(A.pair_m2, __fmul_rn(__fmul_rn(tp.gRf, tp.cvinvf), __fmul_rn(uf[0], eint)));
+        else
+            fast |= A.pair_m2 < 0.f;
     }
     if (bad) {
         atomicOr(A.flag, SHLL_FLAG_NONPOSITIVE);
         if (A.item_flags) atomicOr(&A.item_flags[ch.tube], SHLL_FLAG_NONPOSITIVE);
     }
-    if (ORDER == 1 && A.mode[0]) {
+    if (A.mode[0]) {
         const int any = __syncthreads_or(fast);
         if (tid == 0) ((sweep & 1) ? A.mode[1] : A.mode[0])[ch.id] = any;
     }
@@ -709,13 +742,13 @@ __global__ void __launch_bounds__(MT, 3) k_sweep1d(SweepArgs A) {
 // (each block runs its chunk only when the chunk's pair-flux decision calls for it).  Its own
 // kernel so that the longer double-FP32 step does not raise the register count, and so lower the
 // occupancy, of the FP32 sweeps.
-template <bool KAHAN, bool LAM_POW2>
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
 __global__ void __launch_bounds__(MT, 2) k_sweep1d_ff(SweepArgs A) {
     __shared__ Smem1 S;
     const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];
     float2 dh[3], dl[3];
-    sweep_chunk<1, KAHAN, LAM_POW2, 0, false, true>(A, A.sweep, ch, tp, S, dh, dl, false, false);
+    sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, false, true>(A, A.sweep, ch, tp, S, dh, dl, false, false);
 }
 
 // The pair-flux flags of the state at the start of a run (as sweep -1 would leave them): one block
@@ -730,7 +763,7 @@ __global__ void __launch_bounds__(256) k_mode1d(SweepArgs A) {
     __shared__ float wmax[8], wmin[8];
     const Chunk ch = A.chunks[blockIdx.x];
     const TubeP tp = A.tubes[ch.tube];
-    int fast = 0;
+    int fast = tp.order == 2 && A.pair_m2 < 0.f;   // second order: only where asked for everywhere
     float pmax = 0.f, pmin = 3.0e38f;
     if (tp.order == 1) {
         const void* hin = tp.par ? A.hi[1] : A.hi[0];
@@ -789,7 +822,9 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
 // counters: the buffer that sweep k + 1 writes was read by the neighbours' sweep k, which has
 // completed.  Each wait is bounded: a block that gives up sets SHLL_FLAG_TIMEOUT and returns, and
 // so, bounded again, do the blocks waiting for it.
-template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
+// FM: the flux arithmetic, 0 FP32 (no pair-flux code in the kernel), 1 chosen per chunk and sweep
+// by the pair-flux flags (first order), 2 double-FP32 in every sweep (the pair flux everywhere).
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM>
 __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
     __shared__ Smem1 S;
     __shared__ int s_ok;
@@ -826,16 +861,14 @@ __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
         // sweeps of B steps inside a fold window share the geometry of the one before
         const bool reuse = sw % F != 0 && tp.steps - sw * tp.B >= tp.B;
         const bool keep = sw + 1 < nsw && (sw + 1) % F != 0 && tp.steps - (sw + 1) * tp.B >= tp.B;
-        if constexpr (ORDER == 1) {
-            // the neighbours' flags of the previous sweep are visible after the wait above (they
-            // were written before the neighbours' release); block-uniform
-            if (A.mode[0] && pair_mode(A, ch, sw))
-                sweep_chunk<1, KAHAN, LAM_POW2, LIM, true, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
-            else
-                sweep_chunk<1, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
-        } else {
+        // (FM 1: the neighbours' flags of the previous sweep are visible after the wait above, as
+        // they were written before the neighbours' release; block-uniform)
+        if constexpr (FM == 2)
+            sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+        else if (FM == 1 && A.mode[0] && pair_mode(A, ch, sw))
+            sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true, FM == 1>(A, sw, ch, tp, S, dh, dl, reuse, keep);
+        else
             sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
-        }
         __syncthreads();
         // (the barrier orders the block's stores before thread 0's release at GPU scope)
         if (threadIdx.x == 0 && ch.id != A.stall_id) st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
@@ -906,8 +939,12 @@ static cudaError_t allow_solo_padding() {
         (const void*)k_sweep1d<2, false, false, 0>, (const void*)k_sweep1d<2, true, false, 0>,
         (const void*)k_sweep1d<2, false, true, 1>, (const void*)k_sweep1d<2, true, true, 1>,
         (const void*)k_sweep1d<2, false, false, 1>, (const void*)k_sweep1d<2, true, false, 1>,
-        (const void*)k_sweep1d_ff<false, true>, (const void*)k_sweep1d_ff<true, true>,
-        (const void*)k_sweep1d_ff<false, false>, (const void*)k_sweep1d_ff<true, false>};
+        (const void*)k_sweep1d_ff<1, false, true, 0>, (const void*)k_sweep1d_ff<1, true, true, 0>,
+        (const void*)k_sweep1d_ff<1, false, false, 0>, (const void*)k_sweep1d_ff<1, true, false, 0>,
+        (const void*)k_sweep1d_ff<2, false, true, 0>, (const void*)k_sweep1d_ff<2, true, true, 0>,
+        (const void*)k_sweep1d_ff<2, false, false, 0>, (const void*)k_sweep1d_ff<2, true, false, 0>,
+        (const void*)k_sweep1d_ff<2, false, true, 1>, (const void*)k_sweep1d_ff<2, true, true, 1>,
+        (const void*)k_sweep1d_ff<2, false, false, 1>, (const void*)k_sweep1d_ff<2, true, false, 1>};
     for (const void* k : ks) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSoloSmem);
         if (e != cudaSuccess) return e;
@@ -937,7 +974,7 @@ static cudaError_t launch_sweep(int variant, bool kahan, int grid, cudaStream_t 
 
 // the pair-flux sweep of a first-order variant group (variants 0, 1); its dynamic shared memory
 // holds the remainders of the split fluxes (within the padding when the grid is a single wave)
-template <bool KAHAN, bool LAM_POW2>
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
 static cudaError_t launch_one_ff(int grid, cudaStream_t s, const SweepArgs& A, bool pdl) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -949,34 +986,42 @@ static cudaError_t launch_one_ff(int grid, cudaStream_t s, const SweepArgs& A, b
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_sweep1d_ff<KAHAN, LAM_POW2>, A);
+    return cudaLaunchKernelEx(&cfg, k_sweep1d_ff<ORDER, KAHAN, LAM_POW2, LIM>, A);
 }
 static cudaError_t launch_sweep_ff(int variant, bool kahan, int grid, cudaStream_t s, const SweepArgs& A, bool pdl) {
     switch (variant * 2 + (kahan ? 1 : 0)) {
-        case 0: return launch_one_ff<false, true>(grid, s, A, pdl);
-        case 1: return launch_one_ff<true, true>(grid, s, A, pdl);
-        case 2: return launch_one_ff<false, false>(grid, s, A, pdl);
-        default: return launch_one_ff<true, false>(grid, s, A, pdl);
+        case 0: return launch_one_ff<1, false, true, 0>(grid, s, A, pdl);
+        case 1: return launch_one_ff<1, true, true, 0>(grid, s, A, pdl);
+        case 2: return launch_one_ff<1, false, false, 0>(grid, s, A, pdl);
+        case 3: return launch_one_ff<1, true, false, 0>(grid, s, A, pdl);
+        case 4: return launch_one_ff<2, false, true, 0>(grid, s, A, pdl);
+        case 5: return launch_one_ff<2, true, true, 0>(grid, s, A, pdl);
+        case 6: return launch_one_ff<2, false, false, 0>(grid, s, A, pdl);
+        case 7: return launch_one_ff<2, true, false, 0>(grid, s, A, pdl);
+        case 8: return launch_one_ff<2, false, true, 1>(grid, s, A, pdl);
+        case 9: return launch_one_ff<2, true, true, 1>(grid, s, A, pdl);
+        case 10: return launch_one_ff<2, false, false, 1>(grid, s, A, pdl);
+        default: return launch_one_ff<2, true, false, 1>(grid, s, A, pdl);
     }
 }
 static_assert(kPairSmem <= kSoloSmem, "the pair-flux buffers fit in the padding of single-wave sweeps");
 
 // resident form of a run (k_tube1d): a cooperative launch of one block per chunk, each alone on
 // its SM (the same shared-memory padding as single-wave sweeps)
-template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM>
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM>
 static cudaError_t launch_res(int grid, cudaStream_t s, const SweepArgs& A, unsigned* prog, bool check_only) {
     static unsigned long long attr_set = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 64 && !(attr_set & (1ull << dev))) {
-        cudaError_t e = cudaFuncSetAttribute(k_tube1d<ORDER, KAHAN, LAM_POW2, LIM>,
+        cudaError_t e = cudaFuncSetAttribute(k_tube1d<ORDER, KAHAN, LAM_POW2, LIM, FM>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, kSoloSmem);
         if (e != cudaSuccess) return e;
         attr_set |= 1ull << dev;
     }
     if (check_only) {  // every block must be resident at once
         int per_sm = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM>,
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM, FM>,
                                                                       MT, kSoloSmem);
         if (e != cudaSuccess) return e;
         return (long)per_sm * device_sms() >= grid ? cudaSuccess : cudaErrorCooperativeLaunchTooLarge;
@@ -991,24 +1036,39 @@ static cudaError_t launch_res(int grid, cudaStream_t s, const SweepArgs& A, unsi
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM>, A, prog);
+    return cudaLaunchKernelEx(&cfg, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM, FM>, A, prog);
 }
 
+// all_pairs: the pair flux everywhere (second order then needs the pair-flux kernel; first order
+// chooses per chunk and sweep either way)
 static cudaError_t launch_resident(int variant, bool kahan, int grid, cudaStream_t s, const SweepArgs& A,
-                                   unsigned* prog, bool check_only) {
-    switch (variant * 2 + (kahan ? 1 : 0)) {
-        case 0: return launch_res<1, false, true, 0>(grid, s, A, prog, check_only);
-        case 1: return launch_res<1, true, true, 0>(grid, s, A, prog, check_only);
-        case 2: return launch_res<1, false, false, 0>(grid, s, A, prog, check_only);
-        case 3: return launch_res<1, true, false, 0>(grid, s, A, prog, check_only);
-        case 4: return launch_res<2, false, true, 0>(grid, s, A, prog, check_only);
-        case 5: return launch_res<2, true, true, 0>(grid, s, A, prog, check_only);
-        case 6: return launch_res<2, false, false, 0>(grid, s, A, prog, check_only);
-        case 7: return launch_res<2, true, false, 0>(grid, s, A, prog, check_only);
-        case 8: return launch_res<2, false, true, 1>(grid, s, A, prog, check_only);
-        case 9: return launch_res<2, true, true, 1>(grid, s, A, prog, check_only);
-        case 10: return launch_res<2, false, false, 1>(grid, s, A, prog, check_only);
-        default: return launch_res<2, true, false, 1>(grid, s, A, prog, check_only);
+                                   unsigned* prog, bool check_only, bool all_pairs) {
+    const int v = variant * 2 + (kahan ? 1 : 0);
+    if (variant >= 2 && all_pairs) {
+        switch (v) {
+            case 4: return launch_res<2, false, true, 0, 2>(grid, s, A, prog, check_only);
+            case 5: return launch_res<2, true, true, 0, 2>(grid, s, A, prog, check_only);
+            case 6: return launch_res<2, false, false, 0, 2>(grid, s, A, prog, check_only);
+            case 7: return launch_res<2, true, false, 0, 2>(grid, s, A, prog, check_only);
+            case 8: return launch_res<2, false, true, 1, 2>(grid, s, A, prog, check_only);
+            case 9: return launch_res<2, true, true, 1, 2>(grid, s, A, prog, check_only);
+            case 10: return launch_res<2, false, false, 1, 2>(grid, s, A, prog, check_only);
+            default: return launch_res<2, true, false, 1, 2>(grid, s, A, prog, check_only);
+        }
+    }
+    switch (v) {
+        case 0: return launch_res<1, false, true, 0, 1>(grid, s, A, prog, check_only);
+        case 1: return launch_res<1, true, true, 0, 1>(grid, s, A, prog, check_only);
+        case 2: return launch_res<1, false, false, 0, 1>(grid, s, A, prog, check_only);
+        case 3: return launch_res<1, true, false, 0, 1>(grid, s, A, prog, check_only);
+        case 4: return launch_res<2, false, true, 0, 0>(grid, s, A, prog, check_only);
+        case 5: return launch_res<2, true, true, 0, 0>(grid, s, A, prog, check_only);
+        case 6: return launch_res<2, false, false, 0, 0>(grid, s, A, prog, check_only);
+        case 7: return launch_res<2, true, false, 0, 0>(grid, s, A, prog, check_only);
+        case 8: return launch_res<2, false, true, 1, 0>(grid, s, A, prog, check_only);
+        case 9: return launch_res<2, true, true, 1, 0>(grid, s, A, prog, check_only);
+        case 10: return launch_res<2, false, false, 1, 0>(grid, s, A, prog, check_only);
+        default: return launch_res<2, true, false, 1, 0>(grid, s, A, prog, check_only);
     }
 }
 
@@ -1061,7 +1121,8 @@ struct MixedState {
     float* dh[2] = {nullptr, nullptr};   // deviation pairs between the sweeps of a fold window
     float* dl[2] = {nullptr, nullptr};
     Frame1* frames = nullptr;            // per chunk: frame of the current fold window
-    int* mode[2] = {nullptr, nullptr};   // per chunk, by sweep parity: pair-flux flags (first order)
+    int* mode[2] = {nullptr, nullptr};   // per chunk, by sweep parity: pair-flux flags
+    bool has_first = false;              // a first-order tube (the only ones flagged by default)
     unsigned* prog = nullptr;            // per chunk: sweeps completed in a resident run
     size_t prog_n = 0;
     double* stage = nullptr;             // device staging of one item's primitive planes
@@ -1157,12 +1218,11 @@ static void fix_fold_sweeps(MixedState* m) {
         if (min_owned[t] < m->tubes[t].order * m->tubes[t].B) m->tubes[t].fold_sweeps = 1;
 }
 
-// pair-flux flags per chunk and sweep parity, when a tube is first order
+// pair-flux flags per chunk and sweep parity
 static cudaError_t alloc_mode_flags(MixedState* m) {
     for (int b = 0; b < 2; b++) { cudaFree(m->mode[b]); m->mode[b] = nullptr; }
-    bool first = false;
-    for (const TubeP& tp : m->tubes) first = first || tp.order == 1;
-    if (!first) return cudaSuccess;
+    m->has_first = false;
+    for (const TubeP& tp : m->tubes) m->has_first = m->has_first || tp.order == 1;
     for (int b = 0; b < 2; b++) {
         cudaError_t e = cudaMalloc(&m->mode[b], sizeof(int) * m->chunks.size());
         if (e == cudaSuccess) e = cudaMemset(m->mode[b], 0, sizeof(int) * m->chunks.size());
@@ -1682,10 +1742,11 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
     A.item_flags = m->d_item_flags;
     A.stall_id = resident ? g_stall.load() : -1;
     A.sweep = 0;
-    const bool pairs = g_pair_flux.load() && m->mode[0];
+    const int pf = g_pair_flux.load();
+    const bool pairs = pf && m->mode[0] && (m->has_first || pf == 2);
     A.mode[0] = pairs ? m->mode[0] : nullptr;
     A.mode[1] = pairs ? m->mode[1] : nullptr;
-    A.pair_m2 = g_pair_flux.load() == 2 ? -1.0f : kPairMach * kPairMach;
+    A.pair_m2 = pf == 2 ? -1.0f : kPairMach * kPairMach;
     long n = 0, extra = 0;
     if (pairs) {  // the flags of the state at the start of the run
         A.chunk0 = 0;
@@ -1697,7 +1758,8 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
         A.chunk0 = 0;
         cudaError_t e = cudaMemsetAsync(m->prog, 0, sizeof(unsigned) * kProgStride * order.size(), m->stream);
         if (e == cudaSuccess)
-            e = launch_resident(groups[0].variant, m->kahan, (int)order.size(), m->stream, A, m->prog, false);
+            e = launch_resident(groups[0].variant, m->kahan, (int)order.size(), m->stream, A, m->prog, false,
+                                pairs && pf == 2);
         if (e != cudaSuccess) return e;
         n = 1;
         nsweeps = 0;
@@ -1708,11 +1770,16 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
             const int cnt = g.active[k + 1];
             if (cnt == 0) continue;
             A.chunk0 = g.first;
-            cudaError_t e = launch_sweep(g.variant, m->kahan, cnt, m->stream, A, n > 0);
-            if (e != cudaSuccess) return e;
-            n++;
-            if (pairs && g.variant <= 1) {  // first order: the same chunks' pair-flux form
-                e = launch_sweep_ff(g.variant, m->kahan, cnt, m->stream, A, true);
+            // the FP32 form (not needed when every chunk takes the pair flux), then the same
+            // chunks' pair-flux form (first order, or every order when asked for everywhere)
+            cudaError_t e = cudaSuccess;
+            if (!(pairs && pf == 2)) {
+                e = launch_sweep(g.variant, m->kahan, cnt, m->stream, A, n > 0);
+                if (e != cudaSuccess) return e;
+                n++;
+            }
+            if (pairs && (g.variant <= 1 || pf == 2)) {
+                e = launch_sweep_ff(g.variant, m->kahan, cnt, m->stream, A, n > 0);
                 if (e != cudaSuccess) return e;
                 n++;
             }
@@ -1749,7 +1816,8 @@ static bool resident_run(MixedState* m, const std::vector<Chunk>& order) {
         m->prog_n = order.size();
     }
     SweepArgs none{};
-    if (launch_resident(v, m->kahan, (int)order.size(), m->stream, none, m->prog, true) != cudaSuccess) {
+    if (launch_resident(v, m->kahan, (int)order.size(), m->stream, none, m->prog, true, g_pair_flux.load() == 2) !=
+        cudaSuccess) {
         cudaGetLastError();
         return false;
     }
@@ -2255,21 +2323,23 @@ extern "C" int shll_tube_run_static(const shll_params* p, double* d_cons, long n
     A.chunk0 = 0;
     // first order: the pair-flux flags, as in the context API (two ints per chunk in the array;
     // the start-of-run kernel writes them before the first sweep reads them)
-    const bool pairs = tp.order == 1 && g_pair_flux.load();
+    const int pf = g_pair_flux.load();
+    const bool pairs = pf && (tp.order == 1 || pf == 2);
     A.mode[0] = pairs ? reinterpret_cast<int*>(sc + kStaticModeOff) : nullptr;
     A.mode[1] = pairs ? A.mode[0] + kStaticMaxChunks : nullptr;
-    A.pair_m2 = g_pair_flux.load() == 2 ? -1.0f : kPairMach * kPairMach;
+    A.pair_m2 = pf == 2 ? -1.0f : kPairMach * kPairMach;
     const long nsweeps = (nsteps + B - 1) / B;
     e = allow_solo_padding();
     if (e == cudaSuccess && pairs) {
         k_mode1d<false><<<k, 256, 0, s>>>(A);
         e = cudaGetLastError();
     }
-    shll_count_launches((pairs ? 2 * nsweeps + 1 : nsweeps) + 1);
+    const bool fp32 = !(pairs && pf == 2);   // (every chunk takes the pair flux: no FP32 launches)
+    shll_count_launches(((fp32 ? 1 : 0) + (pairs ? 1 : 0)) * nsweeps + (pairs ? 1 : 0) + 1);
     for (long w = 0; w < nsweeps && e == cudaSuccess; w++) {
         A.sweep = (int)w;
-        e = launch_sweep(tube_variant(tp), false, k, s, A, w > 0);
-        if (e == cudaSuccess && pairs) e = launch_sweep_ff(tube_variant(tp), false, k, s, A, true);
+        if (fp32) e = launch_sweep(tube_variant(tp), false, k, s, A, w > 0);
+        if (e == cudaSuccess && pairs) e = launch_sweep_ff(tube_variant(tp), false, k, s, A, fp32 || w > 0);
     }
     if (e != cudaSuccess) {
         fprintf(stderr, "shll_tube_run_static: sweep launch failed: %s\n", cudaGetErrorString(e));

@@ -344,3 +344,32 @@ __device__ __forceinline__ void flux1x2_ff(const FF2 U[3], FF2 gg1, FF2 gm1, FF2
         fm[k] = ffsub(F[k], fp[k]);
     }
 }
+
+// minmod of two pairs per lane, as the reference's minmod (base-c/2nd_order_base_shll.c:191-201):
+// 0 unless both have the same sign, else the one of smaller magnitude (the second on a tie); a
+// pair's sign is that of its high part and magnitudes compare by high, then low parts
+__device__ __forceinline__ float2 ffsel(bool q0, bool q1, float2 a, float2 b) {
+    return make_float2(q0 ? a.x : b.x, q1 ? a.y : b.y);
+}
+__device__ __forceinline__ FF2 ffminmod(FF2 a, FF2 b) {
+    bool pick_a[2], zero[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const float ah = lane(a.h, q), al = lane(a.l, q), bh = lane(b.h, q), bl = lane(b.l, q);
+        zero[q] = !((ah > 0.f && bh > 0.f) || (ah < 0.f && bh < 0.f));
+        const float sa = ah < 0.f ? -1.f : 1.f, sb = bh < 0.f ? -1.f : 1.f;
+        const float mah = fabsf(ah), mbh = fabsf(bh);
+        pick_a[q] = mah < mbh || (mah == mbh && __fmul_rn(sa, al) < __fmul_rn(sb, bl));
+    }
+    FF2 r = {ffsel(pick_a[0], pick_a[1], a.h, b.h), ffsel(pick_a[0], pick_a[1], a.l, b.l)};
+    r.h = ffsel(zero[0], zero[1], f2(0.f), r.h);
+    r.l = ffsel(zero[0], zero[1], f2(0.f), r.l);
+    return r;
+}
+// limited slope from the differences a = f_j - f_{j-1}, b = f_{j+1} - f_j: minmod (LIM = 0) or the
+// MC limiter minmod((a+b)/2, alpha minmod(a, b)) (LIM = 1, base-omp/2nd_order_base_shll.c:316-325)
+template <int LIM>
+__device__ __forceinline__ FF2 ffslope(FF2 a, FF2 b, float alpha) {
+    if (LIM == 1) return ffminmod(ffscale(ffadd(a, b), 0.5f), ffmul(ffv(alpha, 0.f), ffminmod(a, b)));
+    return ffminmod(a, b);
+}

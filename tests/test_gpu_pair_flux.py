@@ -1,0 +1,89 @@
+"""The pair flux everywhere (shll_set_pair_flux(2)): every chunk of every tube, first and second
+order, evaluates its fluxes, slopes and increments in double-FP32 arithmetic.
+
+The second-order scheme (minmod or MC slopes of the split fluxes, base-c/2nd_order_base_shll.c:
+191-201, 210-277, 438-446) amplifies every per-step rounding error (oracle/noise_floor.py: noise of
+1e-14 injected every 10 steps ends as L1 2.9e-10 at 16384 cells, noise of FP32 size as 7.5e-5), so
+FP32 fluxes sit at L1 ~1e-5..1e-4 from FP64 on long tubes while pair fluxes meet L1(rho, u, T) <=
+1e-6 against the bit-exact FP64 path (the oracle's arithmetic).  Runs are bit-identical between
+the resident and the launch-per-sweep schedules, and conserve mass to 1e-12."""
+import numpy as np
+import pytest
+
+from helpers import batch1d_draws, l1
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def everywhere(shll):
+    shll.set_pair_flux(2)
+    yield
+    shll.set_pair_flux(1)
+
+
+def run(shll, p, resident=True):
+    shll.set_resident(resident)
+    try:
+        c = shll.Context(p)
+        c.init_state()
+        t0 = c.totals()
+        c.run()
+        out, t1 = c.primitives(), c.totals()
+        c.close()
+    finally:
+        shll.set_resident(True)
+    return out, t0, t1
+
+
+def exact(shll, p):
+    q = shll.params(1, p.order, nx=p.nx, precision="f64_exact", t_end=p.t_end, n_steps=p.n_steps, cfl=p.cfl,
+                    limiter=p.limiter, mc_alpha=p.mc_alpha, ic_x_d=p.ic.x_d, ic_rho_l=p.ic.rho_l, ic_T_l=p.ic.T_l,
+                    ic_rho_r=p.ic.rho_r, ic_T_r=p.ic.T_r)
+    return run(shll, q)[0]
+
+
+@pytest.mark.parametrize("order,n,extra", [
+    (2, 16384, {}),                                        # Sod, minmod, lam a power of two
+    (2, 9000, {"cfl": 0.3, "limiter": 1, "mc_alpha": 1.25}),  # MC limiter, lam not a power of two
+    # tube 630 of the seeded batch (density ratio 97.7, temperature ratio 1.89; FP64 with and without
+    # fused multiply-add agree to 2e-12 on it)
+    (1, 4784, {"ic_rho_l": 97.70, "ic_T_l": 1.89, "ic_x_d": 0.0}),
+])
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+def test_pair_flux_everywhere_meets_fp64(shll, everywhere, order, n, extra, prec):
+    if order == 1:   # the seeded tube's exact draws
+        d = batch1d_draws()[630]
+        extra = {"ic_rho_l": d[2], "ic_T_l": d[3], "ic_x_d": d[4]}
+        assert d[1] == n
+    p = shll.params(1, order, nx=n, precision=prec, fold_steps=64, **extra)
+    a, t0, t1 = run(shll, p, resident=True)
+    b, _, _ = run(shll, p, resident=False)
+    assert np.array_equal(a, b)
+    err = l1(a, exact(shll, p))
+    assert np.all(err <= 1e-6), err
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+
+
+def test_sod_65536_second_order_meets_fp64(shll, everywhere):
+    # the benchmark's Sod tube (65536 cells, second order, t = 0.2): FP32 fluxes give L1(rho) 7.3e-5
+    p = shll.params(1, 2, nx=65536, precision="mixed_f64")
+    a, t0, t1 = run(shll, p)
+    err = l1(a, exact(shll, p))
+    assert np.all(err <= 1e-6), err
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+
+
+def test_batch_of_both_orders(shll, everywhere):
+    rng = np.random.default_rng(11)
+    items = []
+    for i in range(10):
+        n = int(rng.integers(300, 3000))
+        items.append(shll.params(1, 1 + i % 2, nx=n, precision="mixed_f64", ic_x_d=float(rng.uniform(0.3, 0.7)),
+                                 ic_rho_l=float(rng.uniform(2, 30)), ic_T_l=float(rng.uniform(0.5, 2))))
+    b = shll.Batch(items)
+    b.run()
+    got = [b.primitives(i) for i in range(len(items))]
+    b.close()
+    for p, g in zip(items, got):
+        assert np.all(l1(g, exact(shll, p)) <= 1e-6), (p.nx, p.order)
