@@ -168,6 +168,9 @@ def items_batch2d(shll, precision, count=256, seed=1, fold=0):
 
 
 def params_single(shll, workload, precision, cells, order, fold):
+    if workload == "omp2d":   # base-omp/2nd_order_base_shll.c:30-44, 147-172 (MC limiter, "Configuration 6")
+        return shll.params(2, 2, nx=cells, ny=cells, precision=precision, t_end=0.3, limiter=1, mc_alpha=1.25,
+                           ic_kind=shll.IC_QUADRANTS2D)
     if workload == "sod1d":
         return shll.params(1, order, nx=cells, precision=precision, t_end=0.2, fold_steps=fold)
     return shll.params(2, 1, nx=cells, ny=cells, precision=precision, n_steps=500, fold_steps=fold,
@@ -183,6 +186,8 @@ def describe(workload, cells, order):
         "batch1d": "4096 independent 1D tubes (seed 0), 256..16384 cells log-uniform, half first / half second "
                    "order, each to t=0.2",
         "batch2d": "256 independent 2D first-order domains (seed 1), 128^2..1024^2, circular diaphragms, 400 steps",
+        "omp2d": f"2D second-order SHLL with the MC limiter (alpha 1.25), {cells}x{cells}, four-quadrant initial data "
+                 f"of base-omp, t=0.3 (plain FP64 on the GPU)",
     }[workload]
 
 
@@ -193,7 +198,7 @@ class Problem:
         self.shll, self.workload, self.stream = shll, workload, stream
         self.precision, self.tune, self.tuned = precision, tune and not fold, False
         self.batch = workload.startswith("batch")
-        self.dim = 2 if workload in ("circle2d", "batch2d") else 1
+        self.dim = 2 if workload in ("circle2d", "batch2d", "omp2d") else 1
         if self.batch:
             gen = items_batch1d if workload == "batch1d" else items_batch2d
             self.items = gen(shll, precision, fold=fold)
@@ -371,6 +376,9 @@ def reference_arm(args, workload, W):
     for i in range(W + args.steps):
         if workload in ("batch1d", "batch2d"):
             v, dt, cores, sample = cpu_batch_sample(workload, 4e9 if workload == "batch1d" else 2e9)
+        elif workload == "omp2d":
+            v, dt, cores = cpu_sample_omp2d(args.cells, 200)
+            sample = f"{args.cells}x{args.cells} cells x 200 time steps per step, FP32 as published, {cores} threads"
         elif workload == "sod1d":
             n = args.cells
             steps = max(50, int(3.0e8 / n))
@@ -404,14 +412,19 @@ def job_value(world, cell_updates_per_run, runs, seconds):
     return world * cell_updates_per_run * runs / seconds
 
 
-DEFAULT_CELLS = {"sod1d": 65536, "circle2d": 4096}
+DEFAULT_CELLS = {"sod1d": 65536, "circle2d": 4096, "omp2d": 1024}
+# the arithmetic each workload is measured in (the 2D mixed engine is first order: the second-order
+# base-omp problem runs the plain FP64 path)
+PRECISION = {"omp2d": "f64"}
 
 
-def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, world, rank, local, extras):
+def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, world, rank, local, extras,
+            precision=None):
     """One workload on this rank's GPU: W untimed runs, then `steps` timed runs (CUDA events on the
     launching stream, L2 flushed before each), the end-to-end leg through the public API with host
     buffers, and (rank 0, extras) the FP64 comparison and the CPU baseline.  Returns the JSON fields."""
-    prob = Problem(shll, workload, args.precision, cells, order, args.fold, stream, tune=not args.no_tune)
+    precision = precision or PRECISION.get(workload, args.precision)
+    prob = Problem(shll, workload, precision, cells, order, args.fold, stream, tune=not args.no_tune)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     for _ in range(W):
         prob.reset()
@@ -445,7 +458,7 @@ def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, w
     hbm, peak_kind = peaks()
     bytes_per_cu = 64.0 if prob.dim == 2 else 48.0
     kernel = {"sod1d": "k_tube1d" if launches <= 3 * steps else "k_sweep1d", "batch1d": "k_sweep1d",
-              "circle2d": "k_step2d", "batch2d": "k_step2d"}[workload]
+              "circle2d": "k_step2d", "batch2d": "k_step2d", "omp2d": "k_step2"}[workload]
     achieved = bytes_per_cu * prob.cu * steps / t_total / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": profile_traffic(kernel, workload), "peak_kind": peak_kind, "kernel": kernel,
@@ -474,7 +487,7 @@ def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, w
         "value": value, "unit": "cell-updates/s", "steps": steps, "warmup": W, "ms_per_step": 1000 * t_total / steps,
         "config": {"workload": describe(workload, cells, order), "name": workload, "cells": cells or None,
                    "order": order if workload == "sod1d" else None, "cell_updates_per_run": prob.cu,
-                   "precision": args.precision, "fold_steps": args.fold or ("autotuned" if prob.tuning() else 64),
+                   "precision": precision, "fold_steps": args.fold or ("autotuned" if prob.tuning() else 64),
                    "tuning": prob.tuning(), "parallelism": f"replicas{world}",
                    "l2": "flushed between runs (256 MB write)"},
         "roofline": roofline,
@@ -483,7 +496,9 @@ def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, w
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if extras and rank == 0:
+    if extras and rank == 0 and workload == "omp2d":
+        out["cpu_baseline"] = cpu_baseline(workload, cells, order)
+    elif extras and rank == 0:
         out.update(fp64_comparison(shll, torch, stream, prob, args, cells, order, mixed_out, t_total / steps))
     prob.close()
     return out
@@ -495,7 +510,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sod1d", choices=["sod1d", "circle2d", "batch1d", "batch2d"])
+    ap.add_argument("--workload", default="sod1d", choices=["sod1d", "circle2d", "batch1d", "batch2d", "omp2d"])
     ap.add_argument("--cells", type=int, default=0, help="cells (1D) or side (2D); default per workload")
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--fold", type=int, default=0, help="fold interval of the mixed path (0 = library default)")
@@ -543,7 +558,7 @@ def main():
                    local, not args.no_extras)
     others = {}
     if workload == "sod1d" and not args.no_other_workloads:
-        for w in ("batch1d", "circle2d", "batch2d"):
+        for w in ("batch1d", "circle2d", "batch2d", "omp2d"):
             others[w] = measure(shll, torch, stream, w, DEFAULT_CELLS.get(w, 0), 1, args, args.other_steps, 3, dist,
                                 world, rank, local, not args.no_extras)
     if rank == 0:
@@ -560,8 +575,51 @@ def main():
         dist.destroy_process_group()
 
 
+def host_cpu():
+    """The host CPU model and its processor count."""
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    try:
+        lscpu = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=5).stdout
+        for line in lscpu.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return f"{model or 'unknown CPU'}, nproc {os.cpu_count()}"
+
+
+def cpu_sample_omp2d(n, steps):
+    """base-omp's own problem on every host thread (the oracle's stages with an OpenMP team, FP32 as
+    published): cell-updates/s, seconds, threads."""
+    O = oracle_mod()
+    threads = O.set_threads(0)
+    try:
+        cfg = O.make_cfg(dim=2, order=2, nx=n, ny=n, real_bits=32, limiter=1, mc_alpha=1.25, n_steps=steps)
+        prim = O.ic_quadrants2d(n, n, 32)
+        t0 = time.perf_counter()
+        O.run(cfg, prim)
+        dt = time.perf_counter() - t0
+    finally:
+        O.set_threads(1)
+    return n * n * steps / dt, dt, threads
+
+
 def cpu_baseline(workload, cells, order):
-    """The CPU port of the reference timed on a bounded sample of the workload, 1 thread."""
+    """The CPU port of the reference timed on a bounded sample of the workload (1 thread; base-omp's
+    problem on every host thread)."""
+    if workload == "omp2d":
+        steps = 200
+        v, dt, threads = cpu_sample_omp2d(cells, steps)
+        return {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                "sample": f"{cells}x{cells} cells x {steps} time steps, FP32 as published, {threads} threads "
+                          f"(base-omp's OpenMP stages), {dt:.1f} s; host {host_cpu()}"}
     if workload in ("sod1d", "batch1d"):
         n = cells if workload == "sod1d" else 4096
         order = order if workload == "sod1d" else 2

@@ -47,6 +47,8 @@ def lib():
         L.oracle_run.restype = ctypes.c_long
         L.oracle_split_fluxes.argtypes = [ctypes.POINTER(OracleCfg), dp, dp, dp, dp, dp]
         L.oracle_split_fluxes.restype = ctypes.c_int
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_set_threads.restype = ctypes.c_int
         L.oracle_count_steps.argtypes = [ctypes.POINTER(OracleCfg)]
         L.oracle_count_steps.restype = ctypes.c_long
         L.oracle_ic_sod.argtypes = [ctypes.c_int] + [ctypes.c_double] * 7 + [dp]
@@ -95,6 +97,11 @@ def split_fluxes(cfg, cons):
     if rc != 0:
         raise ValueError("oracle rejected the configuration")
     return (fp, fm, hp, hm) if cfg.dim == 2 else (fp, fm)
+
+
+def set_threads(n):
+    """Threads of the stage loops (n <= 0: all processors); returns the count in use."""
+    return lib().oracle_set_threads(n)
 
 
 def count_steps(cfg):

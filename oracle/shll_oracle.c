@@ -9,6 +9,17 @@
 #include <string.h>
 #include "shll_oracle.h"
 
+/* Threads of the stage loops (base-omp/2nd_order_base_shll.c:615-653 runs the same stages with an
+ * OpenMP team; every cell of a stage is computed independently of the others, so the results do
+ * not depend on the thread count).  1 unless oracle_set_threads() asks for more. */
+static int g_threads = 1;
+#ifdef _OPENMP
+#include <omp.h>
+#define ORACLE_OMP_FOR _Pragma("omp parallel for if (g_threads > 1) num_threads(g_threads) schedule(static)")
+#else
+#define ORACLE_OMP_FOR
+#endif
+
 #define REAL float
 #define SFX _f32
 #include "shll_oracle_impl.h"
@@ -220,4 +231,14 @@ int oracle_riemann_exact(double g, double R, double rhoL, double uL, double TL,
         prim[i] = rho; prim[n + i] = u; prim[2 * n + i] = pr / (rho * R);
     }
     return it;
+}
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    g_threads = n > 0 ? n : omp_get_num_procs();
+#else
+    (void)n;
+    g_threads = 1;
+#endif
+    return g_threads;
 }

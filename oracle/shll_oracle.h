@@ -44,6 +44,10 @@ long oracle_run(const oracle_cfg* cfg, const double* prim_in, double* prim_out, 
 int oracle_split_fluxes(const oracle_cfg* cfg, const double* cons, double* fp, double* fm,
                         double* hp, double* hm);
 
+/* Threads of the stage loops (OpenMP builds; n <= 0: all processors); returns the count in use
+ * (1 without OpenMP).  Results do not depend on it. */
+int oracle_set_threads(int n);
+
 /* Step count of the reference time loop (time += DT in the chosen type until time >= t_end). */
 long oracle_count_steps(const oracle_cfg* cfg);
 

@@ -91,6 +91,7 @@ static void FN(compute_U_from_P)(FN(ost)* s) {
 /* base-c/base_shll.c:161-177 (1D); base-c/base_shll_2d.c:302-319 (2D) */
 static void FN(compute_P_from_U)(FN(ost)* s) {
     REAL **p = s->p, **u = s->u;
+    ORACLE_OMP_FOR
     for (int c = 0; c < s->n; c++) {
         p[0][c] = u[0][c];
         p[1][c] = u[1][c] / u[0][c];
@@ -108,6 +109,7 @@ static void FN(compute_P_from_U)(FN(ost)* s) {
 /* base-c/base_shll.c:130-159 (1D); base-c/base_shll_2d.c:239-300 (2D) */
 static void FN(compute_F_from_P)(FN(ost)* s) {
     REAL **p = s->p, **u = s->u;
+    ORACLE_OMP_FOR
     for (int c = 0; c < s->n; c++) {
         REAL Z1, Z2, Z3, M, P, f[4], h[4];
         if (s->dim == 1) {
@@ -178,9 +180,10 @@ static void FN(update_o1)(FN(ost)* s) {
     /* sign flips of the reflected split flux, per component */
     const REAL sx1[3] = {-1, 1, -1}, sx2[4] = {-1, 1, -1, -1}, sy2[4] = {-1, -1, 1, -1};
     const REAL* sx = (s->dim == 1) ? sx1 : sx2;
-    REAL Lf[4], Rf[4], Bf[4], Tf[4];
+    ORACLE_OMP_FOR
     for (int i = 0; i < nx; i++) {
         for (int j = 0; j < ny; j++) {
+            REAL Lf[4], Rf[4], Bf[4], Tf[4];
             int idx = i * ny + j;
             for (int k = 0; k < nv; k++) {
                 if (i == 0) { Lf[k] = sx[k] * fm[k][idx]; Rf[k] = fm[k][idx + ny]; }
@@ -212,6 +215,7 @@ static void FN(update_o2)(FN(ost)* s) {
     const int nx = s->nx, ny = s->ny, nv = s->nv, n = s->n;
     REAL **fp = s->fp, **fm = s->fm, **hp = s->hp, **hm = s->hm, **u = s->u;
     /* slopes */
+    ORACLE_OMP_FOR
     for (int i = 0; i < nx; i++) {
         for (int j = 0; j < ny; j++) {
             int idx = i * ny + j;
@@ -233,6 +237,7 @@ static void FN(update_o2)(FN(ost)* s) {
     }
     (void)n;
     /* gather + update (each cell reads only neighbours' fluxes and slopes, never neighbours' U) */
+    ORACLE_OMP_FOR
     for (int i = 0; i < nx; i++) {
         for (int j = 0; j < ny; j++) {
             int idx = i * ny + j;

@@ -108,3 +108,21 @@ def test_oracle_conserves_mass_first_order(oracle):
 def test_oracle_rejects_bad_config(oracle):
     with pytest.raises(ValueError):
         oracle.run(oracle.make_cfg(nx=1), np.ones((3, 1)))
+
+
+def test_threaded_stages_give_the_same_bits(oracle):
+    # base-omp's calling pattern (a team running the stage loops) cannot change a result: every cell
+    # of a stage is computed from the previous stage's arrays only
+    cfg = oracle.make_cfg(dim=2, order=2, nx=96, ny=80, real_bits=32, limiter=1, mc_alpha=1.25, n_steps=40)
+    prim = oracle.ic_quadrants2d(96, 80, 32)
+    _, one, _ = oracle.run(cfg, prim)
+    try:
+        oracle.set_threads(4)
+        _, four, _ = oracle.run(cfg, prim)
+        cfg1 = oracle.make_cfg(dim=2, order=1, nx=64, ny=48, real_bits=64, n_steps=30)
+        _, b4, _ = oracle.run(cfg1, oracle.ic_ref_box2d(64, 48))
+    finally:
+        oracle.set_threads(1)
+    _, b1, _ = oracle.run(cfg1, oracle.ic_ref_box2d(64, 48))
+    assert np.array_equal(one, four)
+    assert np.array_equal(b1, b4)
