@@ -485,6 +485,7 @@ def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, w
     e2e_value = world * prob.cu * len(e_times) / sum(e_times)
     out = {
         "value": value, "unit": "cell-updates/s", "steps": steps, "warmup": W, "ms_per_step": 1000 * t_total / steps,
+        "dtype": {"mixed_f64": "f32-flux+f64-acc", "mixed_kahan": "f32-flux+f32x2-acc"}.get(precision, precision),
         "config": {"workload": describe(workload, cells, order), "name": workload, "cells": cells or None,
                    "order": order if workload == "sod1d" else None, "cell_updates_per_run": prob.cu,
                    "precision": precision, "fold_steps": args.fold or ("autotuned" if prob.tuning() else 64),
@@ -562,10 +563,12 @@ def main():
             others[w] = measure(shll, torch, stream, w, DEFAULT_CELLS.get(w, 0), 1, args, args.other_steps, 3, dist,
                                 world, rank, local, not args.no_extras)
     if rank == 0:
+        head.pop("dtype")
         line = {"metric": "cell-updates/s", "value": head.pop("value"), "unit": head.pop("unit"), "n_gpus": world,
                 "steps": head.pop("steps"), "warmup": head.pop("warmup"), "ms_per_step": head.pop("ms_per_step"),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32-flux+f64-acc" if args.precision == "mixed_f64" else args.precision,
+                "dtype": {"mixed_f64": "f32-flux+f64-acc", "mixed_kahan": "f32-flux+f32x2-acc"}.get(
+                    head["config"]["precision"], head["config"]["precision"]),
                 "data": "synthetic"}
         line.update(head)
         if others:
