@@ -209,10 +209,10 @@ class Problem:
         self.obj = None
 
     def reset(self):
-        """Brings the initial state onto the device (untimed).  1D problems are built once and reset
-        by a device-side restore of the initial state (so repeated runs replay their captured launch
-        sequence); 2D problems are rebuilt."""
-        if self.obj is not None and self.dim == 1:
+        """Brings the initial state onto the device (untimed).  Mixed-precision problems are built
+        once (and autotuned) and reset by a device-side restore of the initial state, so repeated
+        runs replay their captured launch sequence; plain FP64 2D problems are rebuilt."""
+        if self.obj is not None and (self.dim == 1 or self.precision.startswith("mixed")):
             self.obj.restore()
             return
         if self.obj is not None:
@@ -223,15 +223,15 @@ class Problem:
             self.obj = self.shll.Context(self.p)
             self.obj.init_state()
         self.obj.set_stream(self.stream.cuda_stream)
-        if self.dim == 1:
+        if self.dim == 1 or self.precision.startswith("mixed"):
             if self.tune and self.precision.startswith("mixed") and not self.tuned:
-                self.obj.autotune()   # untimed: sweep length and fold window per size class
+                self.obj.autotune()   # untimed: 1D sweep length and fold window per size class, 2D fold window
                 self.tuned = True
             self.obj.checkpoint()
 
     def tuning(self):
         """The autotuner's choices: {"sweep steps/fold steps/chunk cells": items}."""
-        if self.dim != 1 or not self.precision.startswith("mixed"):
+        if not self.precision.startswith("mixed"):
             return None
         if not self.batch:
             return {"%d/%d/%d" % self.obj.tuning(): 1}

@@ -210,9 +210,9 @@ void shll_batch_destroy(shll_batch* b);
 int shll_batch_autotune(shll_batch* b, int trial_steps);
 int shll_batch_tuning(shll_batch* b, int item, int* sweep_steps, int* fold_steps, int* chunk_cells);
 
-/* Device-side checkpoint and restore of a mixed-precision 1D batch (no counterpart in the
+/* Device-side checkpoint and restore of a mixed-precision batch, 1D or 2D (no counterpart in the
  * reference); restore also clears the breakdown flags raised after the checkpoint.
- * SHLL_ERR_UNSUPPORTED for FP64 and 2D batches. */
+ * SHLL_ERR_UNSUPPORTED for FP64 batches. */
 int shll_batch_checkpoint(shll_batch* b);
 int shll_batch_restore(shll_batch* b);
 
@@ -236,14 +236,18 @@ int shll_batch_restore(shll_batch* b);
  * work has completed. */
 int shll_tube_run_static(const shll_params* p, double* d_cons, long nsteps, void* stream);
 
-/* The autotuner for a single mixed-precision 1D context (see shll_batch_autotune). */
+/* The autotuner for a single mixed-precision context (see shll_batch_autotune).  2D (contexts and
+ * batches): the fold window (16, 32, 64 or 128 steps) is timed and chosen for the whole batch and,
+ * process-wide, for its size class (state format, floor(log2 of the largest domain's cells));
+ * shll_tuning / shll_batch_tuning then report sweep 1, that fold window and 512-cell tiles. */
 int shll_autotune(shll_ctx* ctx, int trial_steps);
 int shll_tuning(shll_ctx* ctx, int* sweep_steps, int* fold_steps, int* chunk_cells);
 
-/* Replay of captured launch sequences (no counterpart in the reference): a mixed-precision 1D run
- * is captured into a CUDA graph the first time its step counts and buffer parities occur and the
- * graph is replayed by later identical runs.  on = 0 launches every run directly (default 1;
- * process-wide). */
+/* Replay of captured launch sequences (no counterpart in the reference): a mixed-precision run (1D:
+ * the sweep launches; 2D: the step and fold launches) is captured into a CUDA graph the second time
+ * its step counts (and 1D buffer parities, 2D fold window) occur, and the graph is replayed by later
+ * identical runs; a run that occurs once is launched directly.  Runs on the legacy default stream
+ * are launched directly.  on = 0 launches every run directly (default 1; process-wide). */
 void shll_set_graph_replay(int on);
 
 /* Resident runs (no counterpart in the reference): a mixed-precision 1D run whose chunks fit on

@@ -494,7 +494,7 @@ extern "C" int shll_run(shll_ctx* c, long* steps_taken) {
 
 extern "C" int shll_autotune(shll_ctx* c, int trial_steps) {
     if (!c) return SHLL_ERR_ARG;
-    if (c->plain || c->p.dim != 1) { set_err(c, "the autotuner covers the mixed 1D engine"); return SHLL_ERR_UNSUPPORTED; }
+    if (c->plain) { set_err(c, "the autotuner covers the mixed-precision engines"); return SHLL_ERR_UNSUPPORTED; }
     if (!c->initialized) { set_err(c, "state not initialised (call shll_init_state)"); return SHLL_ERR_STATE; }
     int rc = mixed_autotune(c->mixed, trial_steps, c->err, sizeof(c->err));
     if (rc == SHLL_OK) c->ck_steps = c->steps_taken;   // the device checkpoint now holds this state
@@ -502,7 +502,7 @@ extern "C" int shll_autotune(shll_ctx* c, int trial_steps) {
 }
 
 extern "C" int shll_tuning(shll_ctx* c, int* sweep_steps, int* fold_steps, int* chunk_cells) {
-    if (!c || c->plain || c->p.dim != 1) return SHLL_ERR_ARG;
+    if (!c || c->plain) return SHLL_ERR_ARG;
     return mixed_tuning(c->mixed, 0, sweep_steps, fold_steps, chunk_cells);
 }
 

@@ -1706,6 +1706,8 @@ int mixed_set_item_primitives(MixedState* m, int item, const double* const* plan
 
 static std::atomic<int> g_graph_replay{1};
 extern "C" void shll_set_graph_replay(int on) { g_graph_replay = on ? 1 : 0; }
+bool mixed_graph_replay_on(MixedState* m) { return g_graph_replay.load() != 0 && !m->tuning; }
+void mixed_set_tuning(MixedState* m, bool on) { m->tuning = on; }
 static std::atomic<int> g_resident{1};
 extern "C" void shll_set_resident(int on) { g_resident = on ? 1 : 0; }
 static std::atomic<int> g_stall{-1};
@@ -1938,8 +1940,20 @@ static int rebuild_chunks(MixedState* m, char* err, size_t len) {
 // chunk's owned and halo cells) and the sweeps per FP64 fold window by timing short runs of this
 // batch.  The state is checkpointed first and restored after every trial; the choices are kept
 // in the process-wide table, so later batches and tubes of the same classes start with them.
+int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len);   // mixed2d.cu
+int mixed2d_checkpoint(MixedState* m, bool restore, char* err, size_t len);
+int mixed2d_fold(MixedState* m);
+
 int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
-    if (m->dim != 1) { snprintf(err, len, "the autotuner covers the 1D engine"); return SHLL_ERR_UNSUPPORTED; }
+    if (m->dim == 2) {   // (the trials' cell updates and breakdown flags do not count)
+        const long cu = m->cell_updates;
+        const int rc = mixed2d_autotune(m, trial_steps, err, len);
+        m->cell_updates = cu;
+        if (m->d_flag) cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+        if (m->d_item_flags) cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
+        if (rc == SHLL_OK) m->ck_updates = cu;
+        return rc;
+    }
     long cells = 0;
     double work_total = 0;
     for (const TubeP& tp : m->tubes) { cells += tp.n; work_total += (double)tp.n * tp.n; }
@@ -2051,7 +2065,13 @@ int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
 
 // sweep length and fold interval (steps) and owned cells per chunk chosen for a tube
 int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps, int* chunk_cells) {
-    if (m->dim != 1 || item < 0 || item >= m->nitems) return SHLL_ERR_ARG;
+    if (item < 0 || item >= m->nitems) return SHLL_ERR_ARG;
+    if (m->dim == 2) {   // one step per launch, one fold window for the batch, 16 x 32 tiles
+        if (sweep_steps) *sweep_steps = 1;
+        if (fold_steps) *fold_steps = mixed2d_fold(m);
+        if (chunk_cells) *chunk_cells = 16 * 32;
+        return SHLL_OK;
+    }
     const TubeP& tp = m->tubes[item];
     if (sweep_steps) *sweep_steps = tp.B;
     if (fold_steps) *fold_steps = tp.B * tp.fold_sweeps;
@@ -2151,7 +2171,17 @@ void mixed_add_updates(MixedState* m, long u) { m->cell_updates += u; }
 
 // copies both state buffers (the buffer a tube lives in differs per tube) and the parities
 int mixed_checkpoint(MixedState* m, bool restore, char* err, size_t len) {
-    if (m->dim == 2) { snprintf(err, len, "checkpoint of 2D mixed state not supported"); return SHLL_ERR_UNSUPPORTED; }
+    if (m->dim == 2) {
+        int rc = mixed2d_checkpoint(m, restore, err, len);
+        if (rc == SHLL_OK && restore) {
+            m->cell_updates = m->ck_updates;
+            if (m->d_flag) cudaMemsetAsync(m->d_flag, 0, sizeof(int), m->stream);
+            if (m->d_item_flags) cudaMemsetAsync(m->d_item_flags, 0, sizeof(int) * m->nitems, m->stream);
+        } else if (rc == SHLL_OK) {
+            m->ck_updates = m->cell_updates;
+        }
+        return rc;
+    }
     const size_t vb = (size_t)m->plane * 3 * (m->kahan ? sizeof(float) : sizeof(double));
     const size_t lb = (size_t)m->plane * 3 * sizeof(float);
     if (restore && !m->ck_hi[0]) { snprintf(err, len, "no checkpoint taken"); return SHLL_ERR_STATE; }

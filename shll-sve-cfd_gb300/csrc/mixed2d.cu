@@ -28,6 +28,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "mixed.h"
@@ -42,6 +44,8 @@ void** mixed_d2_slot(MixedState* m);
 bool mixed_is_kahan(MixedState* m);
 void mixed_add_updates(MixedState* m, long u);
 void mixed2d_detach(MixedState* m);
+bool mixed_graph_replay_on(MixedState* m);
+void mixed_set_tuning(MixedState* m, bool on);
 
 namespace {
 
@@ -570,7 +574,29 @@ struct Mixed2D {
     Dom2* d_doms = nullptr;
     TileD* d_tiles = nullptr;
     int fold = 16;
+    // device checkpoint of the stored state (a run starts with a fold that rebuilds frames, C and
+    // the tile constants from it, so the stored state is the whole state between runs)
+    void* ckB = nullptr;
+    float* ckBlo = nullptr;
+    // captured launch sequences of earlier runs (per-domain step counts and fold window), replayed
+    // when a run repeats
+    struct GraphEntry { std::vector<int> steps; int fold; cudaGraphExec_t exec; long launches; };
+    std::vector<GraphEntry> graphs;
+    std::vector<std::pair<std::vector<int>, int>> seen;
 };
+
+// fold windows chosen by the autotuner, process-wide, by (state format, floor(log2 of the largest
+// domain's cells)); applied to later 2D batches whose items leave fold_steps at 0
+static std::mutex g_tune2d_mu;
+static std::map<std::pair<int, int>, int> g_tune2d;
+
+static std::pair<int, int> tune2d_key(const std::vector<Dom2>& doms, bool kahan) {
+    long cells = 1;
+    for (const Dom2& D : doms) cells = std::max(cells, (long)D.nx * D.ny);
+    int lg = 0;
+    while ((2L << lg) <= cells) lg++;
+    return {kahan ? 1 : 0, lg};
+}
 
 static Mixed2D* get2(MixedState* m) { return static_cast<Mixed2D*>(*mixed_d2_slot(m)); }
 int mixed_fold(MixedState* m);
@@ -623,6 +649,11 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
         *mixed_d2_slot(m) = nullptr;
         return nullptr;
     }
+    if (items[0].fold_steps <= 0) {   // a tuned fold window of this class
+        std::lock_guard<std::mutex> lk(g_tune2d_mu);
+        auto it = g_tune2d.find(tune2d_key(d->doms, mixed_is_kahan(m)));
+        if (it != g_tune2d.end()) d->fold = it->second;
+    }
     d->plane = off;
     d->nex = std::max(oex, 1L);
     d->ney = std::max(oey, 1L);
@@ -659,6 +690,9 @@ void mixed2d_detach(MixedState* m) {
     cudaFree(d->tc);
     cudaFree(d->d_doms);
     cudaFree(d->d_tiles);
+    cudaFree(d->ckB);
+    cudaFree(d->ckBlo);
+    for (auto& g : d->graphs) cudaGraphExecDestroy(g.exec);
     delete d;
     *mixed_d2_slot(m) = nullptr;
 }
@@ -678,23 +712,9 @@ int mixed2d_planes(MixedState* m, int item, MixedPlanes* out) {
     return SHLL_OK;
 }
 
-int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
-    Mixed2D* d = get2(m);
-    int count = 0;
-    const shll_params* items = mixed_items(m, &count);
-    long maxsteps = 0, updates = 0;
-    for (int t = 0; t < count; t++) {
-        const long s = nsteps >= 0 ? nsteps : shll_steps_for(&items[t]);
-        d->doms[t].steps = (int)s;
-        maxsteps = std::max(maxsteps, s);
-        updates += s * (long)d->doms[t].nx * d->doms[t].ny;
-    }
-    if (maxsteps == 0) return SHLL_OK;
-    cudaStream_t s = mixed_stream(m);
-    if (cudaMemcpyAsync(d->d_doms, d->doms.data(), sizeof(Dom2) * count, cudaMemcpyHostToDevice, s) != cudaSuccess) {
-        snprintf(err, len, "2D descriptor upload failed");
-        return SHLL_ERR_CUDA;
-    }
+// the launches of one run on stream s: the opening fold, then per step k_step2d and a fold at the
+// end of every window
+static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s) {
     Args2 A;
     memset(&A, 0, sizeof(A));
     A.doms = d->d_doms;
@@ -744,10 +764,149 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
             s0 = (int)(st + 1);
         }
     }
+    return launches;
+}
+
+// Advances every domain by its own step count.  A run whose step counts and fold window occur a
+// second time is captured into a CUDA graph, which later identical runs replay (the descriptors
+// are uploaded before either); a run that occurs once is launched directly.
+int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
+    Mixed2D* d = get2(m);
+    int count = 0;
+    const shll_params* items = mixed_items(m, &count);
+    long maxsteps = 0, updates = 0;
+    std::vector<int> steps(count);
+    for (int t = 0; t < count; t++) {
+        const long s = nsteps >= 0 ? nsteps : shll_steps_for(&items[t]);
+        d->doms[t].steps = (int)s;
+        steps[t] = (int)s;
+        maxsteps = std::max(maxsteps, s);
+        updates += s * (long)d->doms[t].nx * d->doms[t].ny;
+    }
+    if (maxsteps == 0) return SHLL_OK;
+    cudaStream_t s = mixed_stream(m);
+    if (cudaMemcpyAsync(d->d_doms, d->doms.data(), sizeof(Dom2) * count, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+        snprintf(err, len, "2D descriptor upload failed");
+        return SHLL_ERR_CUDA;
+    }
+    long launches = 0;
+    cudaError_t e = cudaSuccess;
+    const bool replay = mixed_graph_replay_on(m) && s != nullptr;   // (the legacy stream cannot be captured)
+    Mixed2D::GraphEntry* hit = nullptr;
+    if (replay)
+        for (auto& g : d->graphs)
+            if (g.steps == steps && g.fold == d->fold) hit = &g;
+    if (hit) {
+        e = cudaGraphLaunch(hit->exec, s);
+        launches = hit->launches;
+    } else {
+        bool repeat = false, done = false;
+        for (auto& k : d->seen) repeat = repeat || (k.first == steps && k.second == d->fold);
+        if (replay && !repeat) {
+            if (d->seen.size() >= 8) d->seen.erase(d->seen.begin());
+            d->seen.push_back({steps, d->fold});
+        }
+        if (replay && repeat) {
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                const long l = issue_run2d(d, m, maxsteps, s);
+                const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+                if (ec == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+                    if (d->graphs.size() >= 4) {
+                        cudaGraphExecDestroy(d->graphs.front().exec);
+                        d->graphs.erase(d->graphs.begin());
+                    }
+                    d->graphs.push_back({steps, d->fold, exec, l});
+                    e = cudaGraphLaunch(exec, s);
+                    launches = l;
+                    done = true;
+                }
+                if (graph) cudaGraphDestroy(graph);
+            }
+            if (!done) cudaGetLastError();   // capture not possible here: launch directly
+        }
+        if (!done) {
+            launches = issue_run2d(d, m, maxsteps, s);
+            e = cudaGetLastError();
+        }
+    }
     shll_count_launches(launches);
-    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { snprintf(err, len, "2D step launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     mixed_add_updates(m, updates);
+    return SHLL_OK;
+}
+
+int mixed2d_fold(MixedState* m) { return get2(m)->fold; }
+
+// copies the stored state (FP64, or the FP32 value and compensation planes) to or from the checkpoint
+int mixed2d_checkpoint(MixedState* m, bool restore, char* err, size_t len) {
+    Mixed2D* d = get2(m);
+    const bool kahan = mixed_is_kahan(m);
+    const size_t nf = (size_t)4 * d->plane;
+    const size_t vb = nf * (kahan ? sizeof(float) : sizeof(double));
+    if (restore && !d->ckB) { snprintf(err, len, "no checkpoint taken"); return SHLL_ERR_STATE; }
+    if (!restore && !d->ckB) {
+        if (cudaMalloc(&d->ckB, vb) != cudaSuccess || (kahan && cudaMalloc(&d->ckBlo, nf * sizeof(float)) != cudaSuccess)) {
+            cudaGetLastError();
+            snprintf(err, len, "checkpoint allocation failed");
+            return SHLL_ERR_NOMEM;
+        }
+    }
+    cudaStream_t s = mixed_stream(m);
+    cudaError_t e = restore ? cudaMemcpyAsync(d->B, d->ckB, vb, cudaMemcpyDeviceToDevice, s)
+                            : cudaMemcpyAsync(d->ckB, d->B, vb, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && kahan)
+        e = restore ? cudaMemcpyAsync(d->Blo, d->ckBlo, nf * sizeof(float), cudaMemcpyDeviceToDevice, s)
+                    : cudaMemcpyAsync(d->ckBlo, d->Blo, nf * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) { snprintf(err, len, "checkpoint copy failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
+    return SHLL_OK;
+}
+
+// Autotuner of the 2D engine: times short runs of the batch (trial_steps steps, best of two, from a
+// checkpoint restored after each) for the fold windows 16, 32, 64 and 128 steps (how many steps
+// the increment pairs accumulate before the stored state absorbs them and the tiles get new frames),
+// keeps the fastest for the batch and, process-wide, for its size class.
+int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
+    Mixed2D* d = get2(m);
+    if (trial_steps <= 0) trial_steps = 128;
+    int rc = mixed2d_checkpoint(m, false, err, len);
+    if (rc != SHLL_OK) return rc;
+    cudaStream_t s = mixed_stream(m);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    mixed_set_tuning(m, true);
+    const int keep = d->fold;
+    int best = keep;
+    float best_ms = 1e30f;
+    for (int f : {16, 32, 64, 128}) {
+        if (f > trial_steps) continue;
+        d->fold = f;
+        float ms = 1e30f;
+        for (int rep = 0; rc == SHLL_OK && rep < 2; rep++) {
+            rc = mixed2d_checkpoint(m, true, err, len);
+            if (rc != SHLL_OK) break;
+            cudaEventRecord(e0, s);
+            rc = mixed2d_run(m, trial_steps, err, len);
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { snprintf(err, len, "trial failed"); rc = SHLL_ERR_CUDA; }
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms = std::min(ms, t);
+        }
+        if (rc != SHLL_OK) break;
+        if (ms < best_ms) { best_ms = ms; best = f; }
+    }
+    mixed_set_tuning(m, false);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    d->fold = rc == SHLL_OK ? best : keep;
+    const int rc2 = mixed2d_checkpoint(m, true, err, len);
+    if (rc != SHLL_OK) return rc;
+    if (rc2 != SHLL_OK) return rc2;
+    std::lock_guard<std::mutex> lk(g_tune2d_mu);
+    g_tune2d[tune2d_key(d->doms, mixed_is_kahan(m))] = best;
     return SHLL_OK;
 }
 

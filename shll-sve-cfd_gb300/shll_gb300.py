@@ -283,7 +283,7 @@ class Context:
         return out
 
     def autotune(self, trial_steps=0):
-        """Picks sweep length and fold window by timed trials (mixed 1D; state restored)."""
+        """Picks the 1D sweep length and fold window, or the 2D fold window, by timed trials (state restored)."""
         return self._ck(lib().shll_autotune(self.h, trial_steps), "autotune")
 
     def tuning(self):

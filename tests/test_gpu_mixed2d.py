@@ -85,3 +85,52 @@ def test_second_order_2d_mixed_is_refused(shll):
     with pytest.raises(shll.ShllError) as e:
         shll.Context(shll.params(2, 2, nx=32, ny=32, precision="mixed_f64"))
     assert e.value.status == shll.ERR_NOMEM or e.value.status == shll.ERR_UNSUPPORTED
+
+
+def test_checkpoint_restore_and_graph_replay(shll):
+    # runs 2 and 3 from the same checkpoint replay a captured graph; all equal the direct launches
+    items = [shll.params(2, 1, nx=n, ny=n, precision="mixed_f64", n_steps=70, ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5,
+                         ic_cy=0.5, ic_radius=0.3, ic_rho_l=9.0, ic_T_l=1.4, ic_rho_r=1.0, ic_T_r=1.0)
+             for n in (48, 96)]
+    import torch
+    s = torch.cuda.Stream()
+    b = shll.Batch(items)
+    b.set_stream(s.cuda_stream)
+    b.checkpoint()
+    outs, launches = [], []
+    for _ in range(3):
+        b.restore()
+        l0 = shll.kernel_launches()
+        b.run()
+        launches.append(shll.kernel_launches() - l0)
+        outs.append([b.primitives(i) for i in range(len(items))])
+    shll.set_graph_replay(False)
+    try:
+        b.restore()
+        b.run()
+        direct = [b.primitives(i) for i in range(len(items))]
+    finally:
+        shll.set_graph_replay(True)
+    b.close()
+    assert launches[0] == launches[1] == launches[2]
+    for o in outs[1:] + [direct]:
+        for x, y in zip(outs[0], o):
+            assert np.array_equal(x, y)
+
+
+def test_autotune_picks_a_fold_window_and_restores_the_state(shll, oracle):
+    n, steps = 80, 120
+    p = shll.params(2, 1, nx=n, ny=n, precision="mixed_f64", n_steps=steps, ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5,
+                    ic_cy=0.5, ic_radius=0.25, ic_rho_l=10.0, ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0)
+    _, ref, _ = oracle.run(oracle.make_cfg(dim=2, order=1, nx=n, ny=n, n_steps=steps),
+                           oracle.ic_circle2d(n, n, r=0.25, rho_in=10.0, rho_out=1.0))
+    b = shll.Batch([p])
+    cu0 = b.cell_updates
+    b.autotune(64)
+    sweep, fold, tile = b.tuning(0)
+    assert (sweep, tile) == (1, 512) and fold in (16, 32, 64)
+    assert b.cell_updates == cu0
+    b.run()
+    assert np.all(l1(b.primitives(0), ref) <= 1e-6)
+    assert b.item_status(0) == 0
+    b.close()
