@@ -272,6 +272,14 @@ void shll_set_resident(int on);
  * at about half the FP32 throughput) (default 1; process-wide). */
 void shll_set_pair_flux(int on);
 
+/* Cluster runs (no counterpart in the reference): a mixed-precision 1D run whose tubes share one
+ * scheme variant and one chunk count of 2 to 16 runs as one launch in which each tube is a
+ * thread-block cluster, the wait between its sweeps being the cluster's hardware barrier instead of
+ * the resident run's neighbour progress counters (the data still passes through L2); the tubes need
+ * not fit on the GPU at once.  Results are identical to the other schedules.  on = 1 enables it
+ * (default 0, a measured alternative; process-wide). */
+void shll_set_cluster_runs(int on);
+
 /* Test hook (no counterpart in the reference): in resident runs the chunk with this index (chunks
  * are numbered along the tubes from 0) never publishes its progress, so its neighbours' bounded
  * waits run out and the run returns SHLL_ERR_TIMEOUT; -1 (the default) switches it off.

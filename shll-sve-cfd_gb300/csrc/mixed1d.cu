@@ -824,8 +824,11 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
 // so, bounded again, do the blocks waiting for it.
 // FM: the flux arithmetic, 0 FP32 (no pair-flux code in the kernel), 1 chosen per chunk and sweep
 // by the pair-flux flags (first order), 2 double-FP32 in every sweep (the pair flux everywhere).
-template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM>
-__global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
+// CLU: the cluster form (k_cluster1d): the chunks of one tube are one thread-block cluster, and the
+// wait between sweeps is the cluster's hardware barrier (release / acquire at cluster scope) instead
+// of the neighbours' progress counters; the data still goes through L2.
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM, bool CLU>
+__device__ __forceinline__ void tube_run(const SweepArgs& A, unsigned* prog) {
     __shared__ Smem1 S;
     __shared__ int s_ok;
     const Chunk ch = A.chunks[A.chunk0 + blockIdx.x];
@@ -834,7 +837,10 @@ __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
     const int F = tp.fold_sweeps;
     float2 dh[3], dl[3];
     for (int sw = 0; sw < nsw; sw++) {
-        if (sw > 0) {
+        if (CLU && sw > 0) {
+            // every block of the cluster (every chunk of the tube) has completed the previous sweep
+            asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+        } else if (sw > 0) {
             if (threadIdx.x == 0) {
                 // both counters polled at once (a chunk without a neighbour on one side reads its
                 // own counter there, which is ahead)
@@ -871,8 +877,22 @@ __global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
             sweep_chunk<ORDER, KAHAN, LAM_POW2, LIM, true>(A, sw, ch, tp, S, dh, dl, reuse, keep);
         __syncthreads();
         // (the barrier orders the block's stores before thread 0's release at GPU scope)
-        if (threadIdx.x == 0 && ch.id != A.stall_id) st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
+        if (!CLU && threadIdx.x == 0 && ch.id != A.stall_id)
+            st_release_gpu(prog + (long)ch.id * kProgStride, (unsigned)(sw + 1));
     }
+}
+
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM>
+__global__ void __launch_bounds__(MT, 1) k_tube1d(SweepArgs A, unsigned* prog) {
+    tube_run<ORDER, KAHAN, LAM_POW2, LIM, FM, false>(A, prog);
+}
+
+// The cluster form of a resident run (launched with one cluster per tube, all tubes of the launch
+// with the same number of chunks, at most 16): no grid-wide residency needed, each tube advances
+// on its own.
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM>
+__global__ void __launch_bounds__(MT, 1) k_cluster1d(SweepArgs A) {
+    tube_run<ORDER, KAHAN, LAM_POW2, LIM, FM, true>(A, nullptr);
 }
 
 // scheme variant of a tube: 0/1 first order (lam a power of two or not), 2/3 second order
@@ -1037,6 +1057,58 @@ static cudaError_t launch_res(int grid, cudaStream_t s, const SweepArgs& A, unsi
     cfg.attrs = at;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k_tube1d<ORDER, KAHAN, LAM_POW2, LIM, FM>, A, prog);
+}
+
+// cluster form: grid = the run's chunks, clusters of `csize` consecutive chunks (one tube each)
+template <int ORDER, bool KAHAN, bool LAM_POW2, int LIM, int FM>
+static cudaError_t launch_clu(int grid, int csize, cudaStream_t s, const SweepArgs& A, bool check_only) {
+    static unsigned long long attr_set = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto* kern = k_cluster1d<ORDER, KAHAN, LAM_POW2, LIM, FM>;
+    if (dev < 64 && !(attr_set & (1ull << dev))) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSoloSmem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+        attr_set |= 1ull << dev;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(MT);
+    cfg.dynamicSmemBytes = kSoloSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (check_only) {   // at least one cluster of this size fits the GPU
+        int n = 0;
+        cudaError_t e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
+        if (e != cudaSuccess) return e;
+        return n >= 1 ? cudaSuccess : cudaErrorInvalidConfiguration;
+    }
+    return cudaLaunchKernelEx(&cfg, kern, A);
+}
+
+static cudaError_t launch_cluster(int variant, bool kahan, int grid, int csize, cudaStream_t s, const SweepArgs& A,
+                                  bool check_only) {
+    switch (variant * 2 + (kahan ? 1 : 0)) {
+        case 0: return launch_clu<1, false, true, 0, 1>(grid, csize, s, A, check_only);
+        case 1: return launch_clu<1, true, true, 0, 1>(grid, csize, s, A, check_only);
+        case 2: return launch_clu<1, false, false, 0, 1>(grid, csize, s, A, check_only);
+        case 3: return launch_clu<1, true, false, 0, 1>(grid, csize, s, A, check_only);
+        case 4: return launch_clu<2, false, true, 0, 0>(grid, csize, s, A, check_only);
+        case 5: return launch_clu<2, true, true, 0, 0>(grid, csize, s, A, check_only);
+        case 6: return launch_clu<2, false, false, 0, 0>(grid, csize, s, A, check_only);
+        case 7: return launch_clu<2, true, false, 0, 0>(grid, csize, s, A, check_only);
+        case 8: return launch_clu<2, false, true, 1, 0>(grid, csize, s, A, check_only);
+        case 9: return launch_clu<2, true, true, 1, 0>(grid, csize, s, A, check_only);
+        case 10: return launch_clu<2, false, false, 1, 0>(grid, csize, s, A, check_only);
+        default: return launch_clu<2, true, false, 1, 0>(grid, csize, s, A, check_only);
+    }
 }
 
 // all_pairs: the pair flux everywhere (second order then needs the pair-flux kernel; first order
@@ -1717,8 +1789,9 @@ extern "C" void shll_set_pair_flux(int on) { g_pair_flux = on == 2 ? 2 : (on ? 1
 
 // issues the launches of one run on m->stream: the sweeps of every variant group (or, resident,
 // one launch for all sweeps of the run's single variant group), then the fix-up
+// cluster > 0: the cluster form of a resident run, clusters of that many chunks (one tube each)
 static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, long nsweeps, long* launches,
-                             bool resident = false) {
+                             bool resident = false, int cluster = 0) {
     struct Group { int variant, first; std::vector<int> active; };
     std::vector<Group> groups;
     for (int c = 0; c < (int)order.size(); c++) {
@@ -1756,7 +1829,13 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
         else k_mode1d<false><<<(unsigned)order.size(), 256, 0, m->stream>>>(A);
         extra++;
     }
-    if (resident) {
+    if (cluster > 0) {
+        A.chunk0 = 0;
+        const cudaError_t e = launch_cluster(groups[0].variant, m->kahan, (int)order.size(), cluster, m->stream, A, false);
+        if (e != cudaSuccess) return e;
+        n = 1;
+        nsweeps = 0;
+    } else if (resident) {
         A.chunk0 = 0;
         cudaError_t e = cudaMemsetAsync(m->prog, 0, sizeof(unsigned) * kProgStride * order.size(), m->stream);
         if (e == cudaSuccess)
@@ -1800,6 +1879,38 @@ static cudaError_t issue_run(MixedState* m, const std::vector<Chunk>& order, lon
 // single-wave, latency-bound case: a tube of up to about 68000 cells), share one scheme variant,
 // and each chunk owns at least the halo width, so that every halo cell comes from an adjacent
 // chunk.  Larger runs keep one launch per sweep, which fills the SMs with several blocks each.
+static std::atomic<int> g_cluster{0};
+extern "C" void shll_set_cluster_runs(int on) { g_cluster = on ? 1 : 0; }
+
+// The cluster form applies when asked for (shll_set_cluster_runs) to runs whose tubes share one scheme
+// variant and one chunk count k (2 <= k <= 16, consecutive in `order`), every chunk owning at least
+// the halo width, and not in the pair flux everywhere; returns k, or 0.
+static int cluster_run(MixedState* m, const std::vector<Chunk>& order) {
+    if (!g_cluster.load() || order.empty() || g_pair_flux.load() == 2) return 0;
+    const int v = tube_variant(m->tubes[order[0].tube]);
+    int k = 0;
+    for (size_t c = 0; c < order.size();) {
+        const int t = order[c].tube;
+        size_t e = c;
+        while (e < order.size() && order[e].tube == t) e++;
+        const int kt = (int)(e - c);
+        if (k == 0) k = kt;
+        if (kt != k || kt < 2 || kt > 16) return 0;
+        for (size_t q = c; q < e; q++) {
+            const TubeP& tp = m->tubes[order[q].tube];
+            if (tube_variant(tp) != v || order[q].b - order[q].a < tp.order * tp.B || order[q].id != order[c].id + (int)(q - c))
+                return 0;
+        }
+        c = e;
+    }
+    SweepArgs none{};
+    if (launch_cluster(v, m->kahan, (int)order.size(), k, m->stream, none, true) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return k;
+}
+
 static bool resident_run(MixedState* m, const std::vector<Chunk>& order) {
     if (!g_resident.load() || order.empty() || (long)order.size() > device_sms()) return false;
     const int v = tube_variant(m->tubes[order[0].tube]);
@@ -1858,9 +1969,10 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
     cudaError_t e = allow_solo_padding();
     if (e != cudaSuccess) { snprintf(err, len, "kernel attribute: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     MixedState::GraphEntry* hit = nullptr;
-    const bool resident = resident_run(m, order);
-    // (a resident run is one launch: nothing to gain from a graph)
-    const bool replay = g_graph_replay.load() != 0 && !m->tuning && !resident;
+    const int cluster = cluster_run(m, order);
+    const bool resident = !cluster && resident_run(m, order);
+    // (a resident or cluster run is one launch: nothing to gain from a graph)
+    const bool replay = g_graph_replay.load() != 0 && !m->tuning && !resident && !cluster;
     if (replay)
         for (auto& g : m->graphs)
             if (g.steps == steps && g.par == m->par) hit = &g;
@@ -1895,7 +2007,7 @@ static int run_tubes(MixedState* m, const std::vector<long>& steps, char* err, s
             }
             if (!done) cudaGetLastError();  // capture not possible here: launch directly
         }
-        if (!done) e = issue_run(m, order, nsweeps, &launches, resident);
+        if (!done) e = issue_run(m, order, nsweeps, &launches, resident, cluster);
     }
     if (e != cudaSuccess) { snprintf(err, len, "sweep launch failed: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     shll_count_launches(launches);

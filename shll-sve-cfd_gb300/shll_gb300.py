@@ -59,6 +59,7 @@ EXPORTS = [
     "shll_batch_restore", "shll_batch_autotune", "shll_batch_tuning", "shll_autotune", "shll_tuning",
     "shll_set_resident", "shll_debug_stall_chunk", "shll_batch_set_primitives", "shll_initial_primitives",
     "shll_batch_set_all_primitives", "shll_batch_get_all_primitives", "shll_set_pair_flux",
+    "shll_set_cluster_runs",
 ]
 
 
@@ -182,6 +183,11 @@ def set_pair_flux(on):
     """Evaluate first-order fluxes in double-FP32 arithmetic where the flow is supersonic (default 1; 0 off,
     2 in every first-order chunk)."""
     lib().shll_set_pair_flux(int(on))
+
+
+def set_cluster_runs(on):
+    """Run 1D tubes of 2..16 chunks as one thread-block cluster each (default off)."""
+    lib().shll_set_cluster_runs(1 if on else 0)
 
 
 def debug_stall_chunk(chunk):

@@ -178,3 +178,36 @@ def test_tuned_sod_tube_resident_equals_launch_per_sweep(shll, oracle):
     assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
     a.close()
     b.close()
+
+
+def _schedules_run(shll, items, cluster=False, resident=True):
+    shll.set_cluster_runs(cluster)
+    shll.set_resident(resident)
+    try:
+        b = shll.Batch(items)
+        l0 = shll.kernel_launches()
+        b.run()
+        launches = shll.kernel_launches() - l0
+        out = [b.primitives(i) for i in range(len(items))]
+        b.close()
+    finally:
+        shll.set_cluster_runs(False)
+        shll.set_resident(True)
+    return out, launches
+
+
+@pytest.mark.parametrize("order,n,count,prec", [(2, 3500, 19, "mixed_f64"), (1, 7000, 5, "mixed_f64"),
+                                               (2, 7000, 3, "mixed_kahan")])
+def test_cluster_runs_equal_the_other_schedules(shll, order, n, count, prec):
+    # tubes of 8 and 16 chunks, each one thread-block cluster with the cluster barrier between
+    # sweeps: the same bits as one launch per sweep and as the resident run
+    rng = np.random.default_rng(order * 100 + count)
+    items = [shll.params(1, order, nx=n, precision=prec, fold_steps=64, n_steps=16 * 40 + 7,
+                         ic_x_d=float(rng.uniform(0.3, 0.7)), ic_rho_l=float(rng.uniform(2, 40)),
+                         ic_T_l=float(rng.uniform(0.5, 2))) for _ in range(count)]
+    a, la = _schedules_run(shll, items, cluster=False, resident=False)
+    b, lb = _schedules_run(shll, items, cluster=True)
+    c, _ = _schedules_run(shll, items, cluster=False, resident=True)
+    assert la > 40 and lb <= 3   # (the cluster run: start-of-run flags, one launch, fix-up)
+    for x, y, z in zip(a, b, c):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
