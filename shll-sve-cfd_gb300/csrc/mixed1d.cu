@@ -2055,6 +2055,7 @@ static int rebuild_chunks(MixedState* m, char* err, size_t len) {
 int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len);   // mixed2d.cu
 int mixed2d_checkpoint(MixedState* m, bool restore, char* err, size_t len);
 int mixed2d_fold(MixedState* m);
+int mixed2d_kstep(MixedState* m);
 
 int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
     if (m->dim == 2) {   // (the trials' cell updates and breakdown flags do not count)
@@ -2178,8 +2179,8 @@ int mixed_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
 // sweep length and fold interval (steps) and owned cells per chunk chosen for a tube
 int mixed_tuning(MixedState* m, int item, int* sweep_steps, int* fold_steps, int* chunk_cells) {
     if (item < 0 || item >= m->nitems) return SHLL_ERR_ARG;
-    if (m->dim == 2) {   // one step per launch, one fold window for the batch, 16 x 32 tiles
-        if (sweep_steps) *sweep_steps = 1;
+    if (m->dim == 2) {   // steps per launch, one fold window for the batch, 16 x 32 tiles
+        if (sweep_steps) *sweep_steps = mixed2d_kstep(m);
         if (fold_steps) *fold_steps = mixed2d_fold(m);
         if (chunk_cells) *chunk_cells = 16 * 32;
         return SHLL_OK;

@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -98,6 +99,7 @@ struct TileC2 {
     float wc[4][4][2];      // constant wall terms: [west, east, south, north][comp][pair]
     float lf[2][4][2];      // lam_x*Fx*, lam_y*Fy* of the frame as pairs
     float dn[4][4][2];      // U*(neighbour) - U*(this) as pairs: [west, east, south, north][comp]
+    float dnd[4][4][2];     // the same for the diagonal neighbours: [(-1,-1), (-1,+1), (+1,-1), (+1,+1)]
     Coef2D cf;              // split-flux coefficients, duplicated into both lanes
 };
 constexpr int kTileC2Words = (int)(sizeof(TileC2) / 4);
@@ -206,10 +208,13 @@ struct Args2 {
     void* B;             // stored state: double[4][plane] or FP32 value planes (KAHAN)
     float* Blo;          // FP32 compensation planes (KAHAN)
     float* C;            // float[4][plane]: B - U*(tile) at the last fold
-    float* Ph[2];        // increment pairs since the last fold, by window-step parity
-    float* Pl[2];
-    Edge* ex[2];         // x / y edge buffers by step parity
-    Edge* ey[2];
+    // increment pairs since the last fold, by window step modulo 3, and the x / y edge records, by
+    // step modulo 3: a launch of one or two steps reads the buffers of its first step and writes
+    // those of its last + 1, never the ones it reads
+    float* Ph[3];
+    float* Pl[3];
+    Edge* ex[3];
+    Edge* ey[3];
     int plane;
     int step;            // global step of a k_step2d launch
     int s0, win;         // fold window: first step and length (k_fold2d)
@@ -223,14 +228,14 @@ __device__ __forceinline__ double loadB(const Args2& A, int idx) {
     return static_cast<const double*>(A.B)[idx];
 }
 
-// edge correction owed to cell (i, j) by the step whose edge buffers have parity pp:
+// edge correction owed to cell (i, j) by the launch whose edge buffers have index pp (0..2):
 // lam*(F of the west/south tile - F of the cell's own tile) on its west / south edge line, as an
 // FP32 pair per component
 __device__ __forceinline__ void edge_correction(const Args2& A, const Dom2& D, int i, int j, int pp, float ch[4],
                                                 float cl[4]) {
     for (int k = 0; k < 4; k++) { ch[k] = 0.f; cl[k] = 0.f; }
     if (i > 0 && i % TI == 0) {
-        const Edge& e = (pp ? A.ex[1] : A.ex[0])[D.ex_base + (i / TI - 1) * D.ny + j];
+        const Edge& e = A.ex[pp][D.ex_base + (i / TI - 1) * D.ny + j];
         for (int k = 0; k < 4; k++) {
             two_sum_acc(ch[k], cl[k], e.r[0][k][0]);
             two_sum_acc(ch[k], cl[k], -e.r[1][k][0]);
@@ -238,7 +243,7 @@ __device__ __forceinline__ void edge_correction(const Args2& A, const Dom2& D, i
         }
     }
     if (j > 0 && j % TJ == 0) {
-        const Edge& e = (pp ? A.ey[1] : A.ey[0])[D.ey_base + (j / TJ - 1) * D.nx + i];
+        const Edge& e = A.ey[pp][D.ey_base + (j / TJ - 1) * D.nx + i];
         for (int k = 0; k < 4; k++) {
             two_sum_acc(ch[k], cl[k], e.r[0][k][0]);
             two_sum_acc(ch[k], cl[k], -e.r[1][k][0]);
@@ -277,9 +282,9 @@ __global__ void __launch_bounds__(NT) k_fold2d(Args2 A) {
     int bad = 0;
     if (own) {
         float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
-        if (wd > 0 && on_edge_line(i, j)) edge_correction(A, D, i, j, (A.s0 + wd - 1) & 1, ch, cl);
-        const float* ph = (wd & 1) ? A.Ph[1] : A.Ph[0];
-        const float* pl = (wd & 1) ? A.Pl[1] : A.Pl[0];
+        if (wd > 0 && on_edge_line(i, j)) edge_correction(A, D, i, j, (A.s0 + wd - 1) % 3, ch, cl);
+        const float* ph = A.Ph[wd % 3];
+        const float* pl = A.Pl[wd % 3];
         for (int k = 0; k < 4; k++) {
             const int idx = k * P + cell;
             if (KAHAN) {
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(NT) k_fold2d(Args2 A) {
 }
 
 // ---- per-tile step constants of the new frames (after a fold) ----
-__global__ void __launch_bounds__(32) k_tileconst2d(Args2 A) {
+__global__ void __launch_bounds__(64) k_tileconst2d(Args2 A) {
     const TileD tile = A.tiles[blockIdx.x];
     const Dom2 D = A.doms[tile.dom];
     const int wd = min(max(D.steps - A.s0, 0), A.win);
@@ -352,6 +357,14 @@ __global__ void __launch_bounds__(32) k_tileconst2d(Args2 A) {
         if (ti >= 0 && ti < D.tiles_i && tj >= 0 && tj < D.tiles_j)
             dU = A.frames[D.tile_base + ti * D.tiles_j + tj].U[k] - f.U[k];
         split2(dU, c.dn[w][k][0], c.dn[w][k][1]);
+    } else if (tid >= 32 && tid < 48) {
+        // the diagonal neighbour w: (ti -/+ 1, tj -/+ 1)
+        const int w = (tid - 32) / 4, k = tid % 4;
+        const int ti = tile.ti + (w < 2 ? -1 : 1), tj = tile.tj + ((w & 1) ? 1 : -1);
+        double dU = 0.0;
+        if (ti >= 0 && ti < D.tiles_i && tj >= 0 && tj < D.tiles_j)
+            dU = A.frames[D.tile_base + ti * D.tiles_j + tj].U[k] - f.U[k];
+        split2(dU, c.dnd[w][k][0], c.dnd[w][k][1]);
     }
 }
 
@@ -369,6 +382,7 @@ struct Smem2 {
     float wc[4][4][2];      // the tile's step constants (a copy of its TileC2)
     float lf[2][4][2];
     float dn[4][4][2];
+    float dnd[4][4][2];
     Coef2D cf;
 };
 
@@ -384,11 +398,11 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
     const int hi_i = min(TI, D.nx - i0), hi_j = min(TJ, D.ny - j0);
     const int P = A.plane;
     const int tb = D.tile_base + tile.ti * D.tiles_j + tile.tj;
-    const float* phi = (kw & 1) ? A.Ph[1] : A.Ph[0];    // increments so far (kw = 0: none)
-    const float* pli = (kw & 1) ? A.Pl[1] : A.Pl[0];
-    float* pho = (kw & 1) ? A.Ph[0] : A.Ph[1];
-    float* plo = (kw & 1) ? A.Pl[0] : A.Pl[1];
-    const int pp = (A.step - 1) & 1;                     // edge buffers of the previous step
+    const float* phi = A.Ph[kw % 3];                     // increments so far (kw = 0: none)
+    const float* pli = A.Pl[kw % 3];
+    float* pho = A.Ph[(kw + 1) % 3];
+    float* plo = A.Pl[(kw + 1) % 3];
+    const int pp = (A.step + 2) % 3;                     // edge buffers of the previous step
     // the tile's step constants and coefficients, one word per thread into shared memory (read
     // from there after the barrier below, which keeps them out of the registers)
     if (tid < kTileC2Words)
@@ -460,8 +474,8 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
     // terms are masked and replaced by the wall terms below
     const bool wS = jx == 0, wNx = jx == D.ny - 1, wNy = has_y && jx + 1 == D.ny - 1;
     const float2 mS = make_float2(wS ? 0.f : 1.f, 1.f), mN = make_float2(wNx ? 0.f : 1.f, wNy ? 0.f : 1.f);
-    Edge* exo = A.step & 1 ? A.ex[1] : A.ex[0];
-    Edge* eyo = A.step & 1 ? A.ey[1] : A.ey[0];
+    Edge* exo = A.ex[A.step % 3];
+    Edge* eyo = A.ey[A.step % 3];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const float2 fp = S.f[k][r][c], fm = S.f[4 + k][r][c], hp = S.f[8 + k][r][c], hm = S.f[12 + k][r][c];
@@ -555,6 +569,259 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
     }
 }
 
+// ---- two time steps of one tile per launch (temporal blocking) ----
+// The tile's window is its 16 x 32 cells plus two cells on every side (20 rows x 18 pairs, the
+// corners included, one thread per pair).  Step 1 evaluates the split fluxes of the whole window and
+// updates every cell whose four neighbours are in it (the tile plus one cell around); step 2
+// evaluates them again and updates the tile's own cells.  The increment pairs are loaded and stored
+// once per two steps; the halo cells are updated in this tile's frame, as in the one-step kernel's
+// halo evaluation.  The edge records are the sums of the two steps' applied fluxes, and the next
+// launch applies the corrections as the one-step kernel does.  A domain with one step left takes one.
+constexpr int NT2 = 384;                      // threads (20 x 18 = 360 window pairs)
+constexpr int WR2 = TI + 4;                   // window rows i0-2 .. i0+TI+1
+constexpr int kStep2Smem = 2 * 16 * WR2 * WP * (int)sizeof(float2);   // flux buffers of the two steps
+
+struct Smem22 {
+    float wc[4][4][2];      // the tile's step constants (a copy of its TileC2)
+    float lf[2][4][2];
+    float dn[4][4][2];
+    float dnd[4][4][2];
+    Coef2D cf;
+    float recx[2][TJ][4][2];   // applied x fluxes summed over the steps: [west edge, east edge][column][comp]
+    float recy[2][TI][4][2];   // applied y fluxes: [south edge, north edge][row][comp]
+};
+static_assert(sizeof(TileC2) == offsetof(Smem22, recx), "the tile constants are copied word for word");
+
+template <bool KAHAN, bool LAM_POW2>
+__global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
+    __shared__ Smem22 S;
+    extern __shared__ __align__(16) float2 g_flux2[];   // [step][16][WR2][WP]
+    const TileD tile = A.tiles[blockIdx.x];
+    const Dom2 D = A.doms[tile.dom];
+    const int ns = min(2, D.steps - A.step);             // steps this domain takes in the launch
+    if (ns <= 0) return;
+    const int tid = threadIdx.x;
+    const int kw = A.step - A.s0;                         // step within the fold window
+    const int i0 = tile.ti * TI, j0 = tile.tj * TJ;
+    const int hi_i = min(TI, D.nx - i0), hi_j = min(TJ, D.ny - j0);
+    const int P = A.plane;
+    const int tb = D.tile_base + tile.ti * D.tiles_j + tile.tj;
+    const float* phi = A.Ph[kw % 3];                      // increments so far (kw = 0: none)
+    const float* pli = A.Pl[kw % 3];
+    float* pho = A.Ph[(kw + ns) % 3];
+    float* plo = A.Pl[(kw + ns) % 3];
+    const int pp = (A.step + 2) % 3;                      // edge buffers of the previous launch
+    Edge* exo = A.ex[(A.step + ns - 1) % 3];
+    Edge* eyo = A.ey[(A.step + ns - 1) % 3];
+    if (tid < kTileC2Words)
+        reinterpret_cast<float*>(&S.wc)[tid] = reinterpret_cast<const float*>(&A.tc[tb])[tid];
+    auto flux = [&](int b, int q, int r, int c) -> float2& { return g_flux2[((b * 16 + q) * WR2 + r) * WP + c]; };
+
+    // ---- this thread's window pair: row wr (cell row i), pair column wc (cells jx, jx + 1) ----
+    const bool pt = tid < WR2 * WP;
+    const int wr = pt ? tid / WP : 0, wc = pt ? tid % WP : 0;
+    const int i = i0 - 2 + wr, jx = j0 - 2 + 2 * wc;
+    bool ex[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) ex[q] = pt && i >= 0 && i < D.nx && jx + q >= 0 && jx + q < D.ny;
+    // owner tile of the pair relative to this one (rows i0-2, i0-1 west, i0+16.. east; pair 0 south,
+    // pair 17 north); -1: this tile
+    const int di = wr < 2 ? -1 : (wr >= 2 + TI ? 1 : 0), dj = wc == 0 ? -1 : (wc == WP - 1 ? 1 : 0);
+    const int nbi = di == 0 && dj == 0 ? -1
+                  : dj == 0 ? (di < 0 ? 0 : 1)
+                  : di == 0 ? (dj < 0 ? 2 : 3)
+                  : 4 + (di < 0 ? 0 : 2) + (dj < 0 ? 0 : 1);
+    // the update regions: step 1 the tile plus one cell around, step 2 (and the stores) the tile
+    const bool r1 = wr >= 1 && wr <= TI + 2;
+    const bool l1[2] = {ex[0] && r1 && jx >= j0 - 1 && jx <= j0 + TJ, ex[1] && r1 && jx + 1 >= j0 - 1 && jx + 1 <= j0 + TJ};
+    const bool ro = wr >= 2 && wr < 2 + hi_i;
+    const bool own[2] = {ex[0] && ro && jx >= j0 && jx < j0 + hi_j, ex[1] && ro && jx + 1 >= j0 && jx + 1 < j0 + hi_j};
+    __syncthreads();   // (the tile constants)
+
+    float2 base[4], ah[4], al[4];   // deviation of the pair at the launch's start, its increments
+#pragma unroll
+    for (int k = 0; k < 4; k++) { base[k] = f2(0.f); ah[k] = f2(0.f); al[k] = f2(0.f); }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (!ex[q]) continue;   // outside the domain: zero deviation (finite fluxes, never applied)
+        const int cell = D.base + i * D.ny + jx + q;
+        float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
+        if (kw > 0 && on_edge_line(i, jx + q)) edge_correction(A, D, i, jx + q, pp, ch, cl);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int idx = k * P + cell;
+            float h = 0.f, l = 0.f;
+            if (kw > 0) { h = phi[idx]; l = pli[idx]; }
+            two_sum_acc(h, l, ch[k]);   // the pending edge correction joins the increment pair
+            l = __fadd_rn(l, cl[k]);
+            set_lane(ah[k], q, h);
+            set_lane(al[k], q, l);
+            // deviation from this tile's frame: C (relative to the owner's frame) + the owner's frame offset
+            float b = A.C[idx];
+            if (nbi >= 0) {
+                const float* o = nbi < 4 ? S.dn[nbi][k] : S.dnd[nbi - 4][k];
+                b = __fadd_rn(__fadd_rn(b, o[0]), o[1]);
+            }
+            set_lane(base[k], q, b);
+        }
+    }
+    // edge records of the tile's own boundary cells (each written only by the cell's owner thread)
+    const bool recW = ro && wr == 2 && i0 > 0, recE = ro && wr == 2 + hi_i - 1 && i + 1 < D.nx;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (!own[q]) continue;
+        const int col = jx + q - j0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (recW) { S.recx[0][col][k][0] = 0.f; S.recx[0][col][k][1] = 0.f; }
+            if (recE) { S.recx[1][col][k][0] = 0.f; S.recx[1][col][k][1] = 0.f; }
+            if (jx + q == j0 && j0 > 0) { S.recy[0][wr - 2][k][0] = 0.f; S.recy[0][wr - 2][k][1] = 0.f; }
+            if (jx + q == j0 + hi_j - 1 && jx + q + 1 < D.ny) { S.recy[1][wr - 2][k][0] = 0.f; S.recy[1][wr - 2][k][1] = 0.f; }
+        }
+    }
+
+    // split fluxes of the pair's current state into buffer b (every thread writes its slot)
+    auto fluxes = [&](int b) {
+        float2 d[4], fp[4], fm[4], hp[4], hm[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) d[k] = add2(base[k], add2(ah[k], al[k]));
+        dflux2x2(S.cf, d, fp, fm, hp, hm);
+        if (pt) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                flux(b, k, wr, wc) = fp[k]; flux(b, 4 + k, wr, wc) = fm[k];
+                flux(b, 8 + k, wr, wc) = hp[k]; flux(b, 12 + k, wr, wc) = hm[k];
+            }
+        }
+    };
+    const float2 lx2 = f2(D.lxh), lxl2 = f2(D.lxl), ly2 = f2(D.lyh), lyl2 = f2(D.lyl);
+    const bool wS = jx == 0, wNx = jx == D.ny - 1, wNy = jx + 1 == D.ny - 1;   // y walls per lane
+    const float2 mS = make_float2(wS ? 0.f : 1.f, 1.f), mN = make_float2(wNx ? 0.f : 1.f, wNy ? 0.f : 1.f);
+    const int cs = max(wc - 1, 0), cn = min(wc + 1, WP - 1);   // (clamped: the lanes they serve are masked)
+    // one step's interface terms from buffer b added to the lanes `up`, the tile's edge records of the
+    // lanes `rec` accumulated
+    auto update = [&](int b, const bool up[2], const bool rec[2]) {
+        auto lam = [&](float2 lh, float2 ll, float2 x, float2& th, float2& tl) {
+            th = mul2(lh, x);
+            tl = LAM_POW2 ? f2(0.f) : add2(fma2(lh, x, neg2(th)), mul2(ll, x));
+        };
+        auto record = [&](float* r, float th, float tl) { two_sum_acc(r[0], r[1], th); r[1] = __fadd_rn(r[1], tl); };
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float2 fp = flux(b, k, wr, wc), fm = flux(b, 4 + k, wr, wc);
+            const float2 hp = flux(b, 8 + k, wr, wc), hm = flux(b, 12 + k, wr, wc);
+            float2 h2 = ah[k], l2 = al[k];
+            auto acc = [&](float2 th, float2 tl) {
+                two_sum_acc2(h2, l2, th);
+                if (!LAM_POW2) l2 = add2(l2, tl);
+            };
+            float2 th, tl;
+            // x west
+            if (i > 0) {
+                lam(lx2, lxl2, add2(flux(b, k, wr - 1, wc), fm), th, tl);
+                acc(th, tl);
+                if (recW)
+                    for (int q = 0; q < 2; q++)
+                        if (rec[q]) record(S.recx[0][jx + q - j0][k], lane(th, q), lane(tl, q));
+            } else {
+                two_sum_acc2(h2, l2, f2(S.wc[0][k][0]));
+                l2 = add2(l2, f2(S.wc[0][k][1]));
+                if (k == 1) { lam(lx2, lxl2, mul2(f2(2.f), fm), th, tl); acc(th, tl); }
+            }
+            // x east
+            if (i < D.nx - 1) {
+                lam(lx2, lxl2, add2(fp, flux(b, 4 + k, wr + 1, wc)), th, tl);
+                acc(neg2(th), neg2(tl));
+                if (recE)
+                    for (int q = 0; q < 2; q++)
+                        if (rec[q]) record(S.recx[1][jx + q - j0][k], lane(th, q), lane(tl, q));
+            } else {
+                two_sum_acc2(h2, l2, f2(S.wc[1][k][0]));
+                l2 = add2(l2, f2(S.wc[1][k][1]));
+                if (k == 1) { lam(lx2, lxl2, mul2(f2(-2.f), fp), th, tl); acc(th, tl); }
+            }
+            // y south: lanes (jx-1 | jx) and (jx | jx+1)
+            {
+                lam(ly2, lyl2, add2(make_float2(flux(b, 8 + k, wr, cs).y, hp.x), hm), th, tl);
+                th = mul2(th, mS); tl = mul2(tl, mS);
+                acc(th, tl);
+                if (rec[0] && jx == j0 && j0 > 0) record(S.recy[0][wr - 2][k], th.x, tl.x);
+            }
+            // y north: lanes (jx | jx+1) and (jx+1 | jx+2)
+            {
+                lam(ly2, lyl2, add2(hp, make_float2(hm.y, flux(b, 12 + k, wr, cn).x)), th, tl);
+                th = mul2(th, mN); tl = mul2(tl, mN);
+                acc(neg2(th), neg2(tl));
+                for (int q = 0; q < 2; q++)
+                    if (rec[q] && jx + q == j0 + hi_j - 1 && jx + q + 1 < D.ny)
+                        record(S.recy[1][wr - 2][k], lane(th, q), lane(tl, q));
+            }
+            // y walls
+            if (wS || wNx || wNy) {
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const bool south = q == 0 && wS, north = q == 0 ? wNx : wNy;
+                    if (!south && !north) continue;
+                    float h = lane(h2, q), l = lane(l2, q);
+                    const int w = south ? 2 : 3;
+                    two_sum_acc(h, l, S.wc[w][k][0]); l = __fadd_rn(l, S.wc[w][k][1]);
+                    if (k == 2) {   // +2 lam_y dhm2 (south), -2 lam_y dhp2 (north)
+                        const float v = south ? __fmul_rn(2.f, lane(hm, q)) : __fmul_rn(-2.f, lane(hp, q));
+                        const float vh = __fmul_rn(D.lyh, v);
+                        const float vl = LAM_POW2 ? 0.f : __fadd_rn(__fmaf_rn(D.lyh, v, -vh), __fmul_rn(D.lyl, v));
+                        two_sum_acc(h, l, vh); l = __fadd_rn(l, vl);
+                    }
+                    set_lane(h2, q, h); set_lane(l2, q, l);
+                }
+            }
+            // only the lanes of the update region change
+            ah[k] = make_float2(up[0] ? h2.x : ah[k].x, up[1] ? h2.y : ah[k].y);
+            al[k] = make_float2(up[0] ? l2.x : al[k].x, up[1] ? l2.y : al[k].y);
+        }
+    };
+
+    fluxes(0);
+    __syncthreads();
+    if (l1[0] || l1[1]) update(0, l1, own);
+    if (ns == 2) {
+        fluxes(1);
+        __syncthreads();
+        if (own[0] || own[1]) update(1, own, own);
+    }
+
+    // ---- the tile's increments and its edge records (full applied fluxes lam Fref ns + the sums) ----
+    const float sc = (float)ns;   // (1 or 2: exact scaling of the pairs)
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (!own[q]) continue;
+        const int cell = D.base + i * D.ny + jx + q;
+        const int col = jx + q - j0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            pho[k * P + cell] = lane(ah[k], q);
+            plo[k * P + cell] = lane(al[k], q);
+            const float lxh = __fmul_rn(sc, S.lf[0][k][0]), lxl = __fmul_rn(sc, S.lf[0][k][1]);
+            const float lyh = __fmul_rn(sc, S.lf[1][k][0]), lyl = __fmul_rn(sc, S.lf[1][k][1]);
+            if (recW) {
+                float* rr = exo[D.ex_base + (i / TI - 1) * D.ny + jx + q].r[1][k];
+                ff_add(lxh, lxl, S.recx[0][col][k][0], S.recx[0][col][k][1], rr[0], rr[1]);
+            }
+            if (recE) {
+                float* rr = exo[D.ex_base + ((i + 1) / TI - 1) * D.ny + jx + q].r[0][k];
+                ff_add(lxh, lxl, S.recx[1][col][k][0], S.recx[1][col][k][1], rr[0], rr[1]);
+            }
+            if (jx + q == j0 && j0 > 0) {
+                float* rr = eyo[D.ey_base + (j0 / TJ - 1) * D.nx + i].r[1][k];
+                ff_add(lyh, lyl, S.recy[0][wr - 2][k][0], S.recy[0][wr - 2][k][1], rr[0], rr[1]);
+            }
+            if (jx + q == j0 + hi_j - 1 && jx + q + 1 < D.ny) {
+                float* rr = eyo[D.ey_base + ((jx + q + 1) / TJ - 1) * D.nx + i].r[0][k];
+                ff_add(lyh, lyl, S.recy[1][wr - 2][k][0], S.recy[1][wr - 2][k][1], rr[0], rr[1]);
+            }
+        }
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
@@ -565,30 +832,31 @@ struct Mixed2D {
     void* B = nullptr;
     float* Blo = nullptr;
     float* C = nullptr;
-    float* Ph[2] = {nullptr, nullptr};
-    float* Pl[2] = {nullptr, nullptr};
-    Edge* ex[2] = {nullptr, nullptr};
-    Edge* ey[2] = {nullptr, nullptr};
+    float* Ph[3] = {nullptr, nullptr, nullptr};
+    float* Pl[3] = {nullptr, nullptr, nullptr};
+    Edge* ex[3] = {nullptr, nullptr, nullptr};
+    Edge* ey[3] = {nullptr, nullptr, nullptr};
     Frame2* frames = nullptr;
     TileC2* tc = nullptr;
     Dom2* d_doms = nullptr;
     TileD* d_tiles = nullptr;
     int fold = 16;
+    int kstep = 1;          // time steps per step launch (k_step2d2 for 2, k_step2d for 1)
     // device checkpoint of the stored state (a run starts with a fold that rebuilds frames, C and
     // the tile constants from it, so the stored state is the whole state between runs)
     void* ckB = nullptr;
     float* ckBlo = nullptr;
     // captured launch sequences of earlier runs (per-domain step counts and fold window), replayed
     // when a run repeats
-    struct GraphEntry { std::vector<int> steps; int fold; cudaGraphExec_t exec; long launches; };
+    struct GraphEntry { std::vector<int> steps; int fold, kstep; cudaGraphExec_t exec; long launches; };
     std::vector<GraphEntry> graphs;
-    std::vector<std::pair<std::vector<int>, int>> seen;
+    std::vector<std::pair<std::vector<int>, int>> seen;   // (step counts, fold * 4 + kstep)
 };
 
 // fold windows chosen by the autotuner, process-wide, by (state format, floor(log2 of the largest
 // domain's cells)); applied to later 2D batches whose items leave fold_steps at 0
 static std::mutex g_tune2d_mu;
-static std::map<std::pair<int, int>, int> g_tune2d;
+static std::map<std::pair<int, int>, std::pair<int, int>> g_tune2d;   // -> (fold window, steps per launch)
 
 static std::pair<int, int> tune2d_key(const std::vector<Dom2>& doms, bool kahan) {
     long cells = 1;
@@ -652,7 +920,7 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
     if (items[0].fold_steps <= 0) {   // a tuned fold window of this class
         std::lock_guard<std::mutex> lk(g_tune2d_mu);
         auto it = g_tune2d.find(tune2d_key(d->doms, mixed_is_kahan(m)));
-        if (it != g_tune2d.end()) d->fold = it->second;
+        if (it != g_tune2d.end()) { d->fold = it->second.first; d->kstep = it->second.second; }
     }
     d->plane = off;
     d->nex = std::max(oex, 1L);
@@ -662,7 +930,7 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
     bool ok = cudaMalloc(&d->B, nf * (kahan ? sizeof(float) : sizeof(double))) == cudaSuccess;
     if (ok && kahan) ok = cudaMalloc(&d->Blo, nf * sizeof(float)) == cudaSuccess;
     if (ok) ok = cudaMalloc(&d->C, nf * sizeof(float)) == cudaSuccess;
-    for (int b = 0; b < 2 && ok; b++) {
+    for (int b = 0; b < 3 && ok; b++) {
         ok = cudaMalloc(&d->Ph[b], nf * sizeof(float)) == cudaSuccess;
         if (ok) ok = cudaMalloc(&d->Pl[b], nf * sizeof(float)) == cudaSuccess;
         if (ok) ok = cudaMalloc(&d->ex[b], sizeof(Edge) * d->nex) == cudaSuccess;
@@ -685,7 +953,7 @@ void mixed2d_detach(MixedState* m) {
     Mixed2D* d = get2(m);
     if (!d) return;
     cudaFree(d->B); cudaFree(d->Blo); cudaFree(d->C);
-    for (int b = 0; b < 2; b++) { cudaFree(d->Ph[b]); cudaFree(d->Pl[b]); cudaFree(d->ex[b]); cudaFree(d->ey[b]); }
+    for (int b = 0; b < 3; b++) { cudaFree(d->Ph[b]); cudaFree(d->Pl[b]); cudaFree(d->ex[b]); cudaFree(d->ey[b]); }
     cudaFree(d->frames);
     cudaFree(d->tc);
     cudaFree(d->d_doms);
@@ -722,10 +990,10 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
     A.frames = d->frames;
     A.tc = d->tc;
     A.B = d->B; A.Blo = d->Blo; A.C = d->C;
-    A.Ph[0] = d->Ph[0]; A.Ph[1] = d->Ph[1];
-    A.Pl[0] = d->Pl[0]; A.Pl[1] = d->Pl[1];
-    A.ex[0] = d->ex[0]; A.ex[1] = d->ex[1];
-    A.ey[0] = d->ey[0]; A.ey[1] = d->ey[1];
+    for (int b = 0; b < 3; b++) {
+        A.Ph[b] = d->Ph[b]; A.Pl[b] = d->Pl[b];
+        A.ex[b] = d->ex[b]; A.ey[b] = d->ey[b];
+    }
     A.plane = (int)d->plane;
     A.flag = mixed_flag_ptr(m);
     A.item_flags = mixed_item_flags_ptr(m);
@@ -737,7 +1005,7 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
         A.win = win;
         if (kahan) k_fold2d<true><<<ntiles, NT, 0, s>>>(A);
         else k_fold2d<false><<<ntiles, NT, 0, s>>>(A);
-        k_tileconst2d<<<ntiles, 32, 0, s>>>(A);
+        k_tileconst2d<<<ntiles, 64, 0, s>>>(A);
         launches += 2;
     };
     // lam_x and lam_y powers of two for every domain: the interface terms lam*Delta are exact
@@ -748,10 +1016,21 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
     }
     fold(0, 0);  // frames and C of the current state
     int s0 = 0;
-    for (long st = 0; st < maxsteps; st++) {
+    for (long st = 0; st < maxsteps;) {
         A.step = (int)st;
         A.s0 = s0;
-        if (kahan) {
+        // two steps per launch inside a fold window, one for an odd remainder
+        const long wend = std::min<long>(s0 + d->fold, maxsteps);
+        const int k = d->kstep == 2 && wend - st >= 2 ? 2 : 1;
+        if (k == 2) {
+            if (kahan) {
+                if (pow2) k_step2d2<true, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
+                else k_step2d2<true, false><<<ntiles, NT2, kStep2Smem, s>>>(A);
+            } else {
+                if (pow2) k_step2d2<false, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
+                else k_step2d2<false, false><<<ntiles, NT2, kStep2Smem, s>>>(A);
+            }
+        } else if (kahan) {
             if (pow2) k_step2d<true, true><<<ntiles, NTP, 0, s>>>(A);
             else k_step2d<true, false><<<ntiles, NTP, 0, s>>>(A);
         } else {
@@ -759,12 +1038,29 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
             else k_step2d<false, false><<<ntiles, NTP, 0, s>>>(A);
         }
         launches++;
-        if (st + 1 - s0 == d->fold || st + 1 == maxsteps) {
-            fold(s0, (int)(st + 1 - s0));
-            s0 = (int)(st + 1);
+        st += k;
+        if (st == wend) {
+            fold(s0, (int)(st - s0));
+            s0 = (int)st;
         }
     }
     return launches;
+}
+
+// allows the two-step kernel its dynamic shared memory on the current device (before any capture)
+static cudaError_t allow_step2_smem() {
+    static unsigned long long done = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev >= 64 || (done & (1ull << dev))) return e;
+    const void* ks[] = {(const void*)k_step2d2<false, false>, (const void*)k_step2d2<false, true>,
+                        (const void*)k_step2d2<true, false>, (const void*)k_step2d2<true, true>};
+    for (const void* k : ks) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kStep2Smem);
+        if (e != cudaSuccess) return e;
+    }
+    done |= 1ull << dev;
+    return cudaSuccess;
 }
 
 // Advances every domain by its own step count.  A run whose step counts and fold window occur a
@@ -790,21 +1086,23 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
         return SHLL_ERR_CUDA;
     }
     long launches = 0;
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = allow_step2_smem();
+    if (e != cudaSuccess) { snprintf(err, len, "kernel attribute: %s", cudaGetErrorString(e)); return SHLL_ERR_CUDA; }
     const bool replay = mixed_graph_replay_on(m) && s != nullptr;   // (the legacy stream cannot be captured)
+    const int key = d->fold * 4 + d->kstep;
     Mixed2D::GraphEntry* hit = nullptr;
     if (replay)
         for (auto& g : d->graphs)
-            if (g.steps == steps && g.fold == d->fold) hit = &g;
+            if (g.steps == steps && g.fold == d->fold && g.kstep == d->kstep) hit = &g;
     if (hit) {
         e = cudaGraphLaunch(hit->exec, s);
         launches = hit->launches;
     } else {
         bool repeat = false, done = false;
-        for (auto& k : d->seen) repeat = repeat || (k.first == steps && k.second == d->fold);
+        for (auto& k : d->seen) repeat = repeat || (k.first == steps && k.second == key);
         if (replay && !repeat) {
             if (d->seen.size() >= 8) d->seen.erase(d->seen.begin());
-            d->seen.push_back({steps, d->fold});
+            d->seen.push_back({steps, key});
         }
         if (replay && repeat) {
             cudaGraph_t graph = nullptr;
@@ -817,7 +1115,7 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
                         cudaGraphExecDestroy(d->graphs.front().exec);
                         d->graphs.erase(d->graphs.begin());
                     }
-                    d->graphs.push_back({steps, d->fold, exec, l});
+                    d->graphs.push_back({steps, d->fold, d->kstep, exec, l});
                     e = cudaGraphLaunch(exec, s);
                     launches = l;
                     done = true;
@@ -838,6 +1136,7 @@ int mixed2d_run(MixedState* m, long nsteps, char* err, size_t len) {
 }
 
 int mixed2d_fold(MixedState* m) { return get2(m)->fold; }
+int mixed2d_kstep(MixedState* m) { return get2(m)->kstep; }
 
 // copies the stored state (FP64, or the FP32 value and compensation planes) to or from the checkpoint
 int mixed2d_checkpoint(MixedState* m, bool restore, char* err, size_t len) {
@@ -865,8 +1164,9 @@ int mixed2d_checkpoint(MixedState* m, bool restore, char* err, size_t len) {
 
 // Autotuner of the 2D engine: times short runs of the batch (trial_steps steps, best of two, from a
 // checkpoint restored after each) for the fold windows 16, 32, 64 and 128 steps (how many steps
-// the increment pairs accumulate before the stored state absorbs them and the tiles get new frames),
-// keeps the fastest for the batch and, process-wide, for its size class.
+// the increment pairs accumulate before the stored state absorbs them and the tiles get new frames)
+// with one or two time steps per step launch, keeps the fastest for the batch and, process-wide,
+// for its size class.
 int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
     Mixed2D* d = get2(m);
     if (trial_steps <= 0) trial_steps = 128;
@@ -877,12 +1177,14 @@ int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     mixed_set_tuning(m, true);
-    const int keep = d->fold;
-    int best = keep;
+    const int keep = d->fold, keepk = d->kstep;
+    int best = keep, bestk = keepk;
     float best_ms = 1e30f;
-    for (int f : {16, 32, 64, 128}) {
+    for (int cand = 0; cand < 8; cand++) {
+        const int f = 16 << (cand / 2), kk = 1 + cand % 2;
         if (f > trial_steps) continue;
         d->fold = f;
+        d->kstep = kk;
         float ms = 1e30f;
         for (int rep = 0; rc == SHLL_OK && rep < 2; rep++) {
             rc = mixed2d_checkpoint(m, true, err, len);
@@ -896,17 +1198,18 @@ int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
             ms = std::min(ms, t);
         }
         if (rc != SHLL_OK) break;
-        if (ms < best_ms) { best_ms = ms; best = f; }
+        if (ms < best_ms) { best_ms = ms; best = f; bestk = kk; }
     }
     mixed_set_tuning(m, false);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     d->fold = rc == SHLL_OK ? best : keep;
+    d->kstep = rc == SHLL_OK ? bestk : keepk;
     const int rc2 = mixed2d_checkpoint(m, true, err, len);
     if (rc != SHLL_OK) return rc;
     if (rc2 != SHLL_OK) return rc2;
     std::lock_guard<std::mutex> lk(g_tune2d_mu);
-    g_tune2d[tune2d_key(d->doms, mixed_is_kahan(m))] = best;
+    g_tune2d[tune2d_key(d->doms, mixed_is_kahan(m))] = {best, bestk};
     return SHLL_OK;
 }
 
