@@ -27,6 +27,7 @@ UNITS = {
     "reduce.cu": [],
     "plain_batch.cu": [],
     "plain_batch_exact.cu": ["-fmad=false"],
+    "refglobals.cu": [],
 }
 HEADERS = ["shll_internal.h", "shll_plain.cuh", "mixed.h", "mixed_common.cuh", "plain_batch.h",
            "plain_batch_kernels.cuh"]
@@ -79,6 +80,15 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    # a reference-style program whose main() is unchanged: it takes the stage functions from the
+    # library, which reads its problem constants and sets its DT
+    drv = os.path.join(BUILD, "shll_ref_main")
+    src = os.path.join(HERE, "host", "shll_ref_main.c")
+    if _stale(drv, [src, LIB]):
+        cmd = ["gcc", "-O2", "-Wall"] + inc + [src, "-o", drv] + link + ["-lshll_gb300"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference-style program build failed:\n{r.stderr}")
     # team-aware stages (OpenMP, base-omp's calling pattern) and their driver; skipped with a
     # message where the C compiler has no OpenMP
     omp_lib = os.path.join(BUILD, "libshll_gb300_omp.so")

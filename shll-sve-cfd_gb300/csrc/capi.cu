@@ -643,6 +643,7 @@ extern "C" int shll_save_results(shll_ctx* c, const char* path) {
 // ---------------- the reference's entry points on a default context ----------------
 static shll_params g_ref_params;
 static bool g_ref_configured = false;
+static bool g_ref_program = false;   // configured from the loading program's reference globals
 static shll_ctx* g_ref = nullptr;
 
 extern "C" int shll_ref_configure(const shll_params* p) {
@@ -661,7 +662,12 @@ static void ref_fail(const char* what, int rc) {
 }
 
 extern "C" void Allocate_and_Init_Memory(void) {
-    if (!g_ref_configured) { shll_params_default(&g_ref_params, 1, 1); g_ref_configured = true; }
+    if (!g_ref_configured) {
+        // a reference program linked against the library: its own problem; else base_shll.c's defaults
+        g_ref_program = shll_ref_program_params(&g_ref_params);
+        if (!g_ref_program) shll_params_default(&g_ref_params, 1, 1);
+        g_ref_configured = true;
+    }
     if (g_ref) { shll_destroy(g_ref); g_ref = nullptr; }
     int rc = shll_create(&g_ref_params, &g_ref);
     if (rc != SHLL_OK) { ref_fail("Allocate_and_Init_Memory", rc); return; }
@@ -684,7 +690,13 @@ extern "C" void Allocate_and_Init_Memory(void) {
         int rc = CALL(g_ref);                                      \
         if (rc != SHLL_OK) ref_fail(#NAME, rc);                    \
     }
-REF_STAGE(Compute_U_from_P, shll_compute_U_from_P)
+extern "C" void Compute_U_from_P(void) {
+    if (!g_ref) { fprintf(stderr, "Compute_U_from_P: no state\n"); return; }
+    int rc = shll_compute_U_from_P(g_ref);
+    if (rc != SHLL_OK) ref_fail("Compute_U_from_P", rc);
+    // and, as the reference's, the step globals that its main() reads
+    if (g_ref_program) shll_ref_set_step(g_ref->DT, g_ref->DT_ON_DX, g_ref->DT_ON_DY);
+}
 REF_STAGE(Compute_P_from_U, shll_compute_P_from_U)
 REF_STAGE(Compute_F_from_P, shll_compute_F_from_P)
 REF_STAGE(Update_U_from_F, shll_update_U_from_F)

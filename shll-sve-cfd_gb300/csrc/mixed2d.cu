@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -825,6 +826,13 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
+// steps per step launch of a new 2D state until the tuner chooses (SHLL_2D_STEPS_PER_LAUNCH = 1 or 2
+// overrides the library's default, 2)
+static int default_kstep() {
+    const char* v = getenv("SHLL_2D_STEPS_PER_LAUNCH");
+    return v && v[0] == '1' ? 1 : 2;
+}
+
 struct Mixed2D {
     std::vector<Dom2> doms;
     std::vector<TileD> tiles;
@@ -841,7 +849,7 @@ struct Mixed2D {
     Dom2* d_doms = nullptr;
     TileD* d_tiles = nullptr;
     int fold = 16;
-    int kstep = 1;          // time steps per step launch (k_step2d2 for 2, k_step2d for 1)
+    int kstep = default_kstep();   // time steps per step launch (k_step2d2 for 2, k_step2d for 1)
     // device checkpoint of the stored state (a run starts with a fold that rebuilds frames, C and
     // the tile constants from it, so the stored state is the whole state between runs)
     void* ckB = nullptr;

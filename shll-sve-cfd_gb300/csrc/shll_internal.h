@@ -13,6 +13,10 @@ struct shll_params;
 // the parameter checks of shll_create (SHLL_OK, or SHLL_ERR_ARG with a message in err)
 int shll_validate_params(const shll_params* p, char* err, size_t len);
 
+// the reference program's globals, when the loading program defines them (refglobals.cu)
+bool shll_ref_program_params(shll_params* p);
+void shll_ref_set_step(double dt, double dtdx, double dtdy);
+
 // kernel launches issued by the library (shll_kernel_launches)
 void shll_count_launches(long n);
 

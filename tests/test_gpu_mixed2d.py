@@ -128,9 +128,55 @@ def test_autotune_picks_a_fold_window_and_restores_the_state(shll, oracle):
     cu0 = b.cell_updates
     b.autotune(64)
     sweep, fold, tile = b.tuning(0)
-    assert (sweep, tile) == (1, 512) and fold in (16, 32, 64)
+    # (the first value: time steps per step launch, one or two)
+    assert sweep in (1, 2) and tile == 512 and fold in (16, 32, 64)
     assert b.cell_updates == cu0
     b.run()
     assert np.all(l1(b.primitives(0), ref) <= 1e-6)
     assert b.item_status(0) == 0
     b.close()
+
+
+
+def _domains_run(shll, items, kstep, monkeypatch):
+    # SHLL_2D_STEPS_PER_LAUNCH sets how many time steps a step launch takes for states created
+    # while it is set (the fold window is given, so no tuned choice replaces it)
+    monkeypatch.setenv("SHLL_2D_STEPS_PER_LAUNCH", str(kstep))
+    b = shll.Batch(items)
+    assert b.tuning(0)[0] == kstep
+    t0 = [b.totals(i) for i in range(len(items))]
+    b.run()
+    out = [b.primitives(i) for i in range(len(items))]
+    t1 = [b.totals(i) for i in range(len(items))]
+    b.close()
+    return out, t0, t1
+
+
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+@pytest.mark.parametrize("fold", [16, 64])
+def test_two_steps_per_launch_vs_fp64_oracle(shll, oracle, monkeypatch, prec, fold):
+    # the two-step kernel (a 20x36 window, the halo cells' first step taken in the tile's own frame,
+    # the edge corrections of both steps applied by the next launch) rounds differently from one
+    # step per launch; both stay within the tolerance of the FP64 oracle and conserve mass and
+    # energy.  Domains smaller and larger than a window, odd step counts (a last single step), a
+    # fold window cut by the run's end.
+    rng = np.random.default_rng(fold)
+    items, refs = [], []
+    for nx, ny, k in ((7, 5, 33), (20, 36, 40), (93, 61, 101), (160, 144, 77), (2, 300, 64)):
+        cx, cy = float(rng.uniform(0.3, 0.7)), float(rng.uniform(0.3, 0.7))
+        r, rin = float(rng.uniform(0.1, 0.3)), float(rng.uniform(2, 10))
+        items.append(shll.params(2, 1, nx=nx, ny=ny, precision=prec, n_steps=k, fold_steps=fold,
+                                 ic_kind=shll.IC_CIRCLE2D, ic_cx=cx, ic_cy=cy, ic_radius=r, ic_rho_l=rin,
+                                 ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0))
+        cfg = oracle.make_cfg(dim=2, order=1, nx=nx, ny=ny, n_steps=k)
+        refs.append(oracle.run(cfg, oracle.ic_circle2d(nx, ny, cx=cx, cy=cy, r=r, rho_in=rin))[1])
+    outs = {}
+    for kstep in (1, 2):
+        out, t0, t1 = _domains_run(shll, items, kstep, monkeypatch)
+        for i in range(len(items)):
+            assert np.all(l1(out[i], refs[i]) <= 1e-6), (kstep, i)
+            for q in (0, 3):
+                assert abs(t1[i][q] - t0[i][q]) / t0[i][q] <= 1e-12, (kstep, i, q)
+        outs[kstep] = out
+    for a, b in zip(outs[1], outs[2]):
+        assert np.all(l1(a, b) <= 1e-6)
