@@ -187,7 +187,7 @@ def describe(workload, cells, order):
                    "order, each to t=0.2",
         "batch2d": "256 independent 2D first-order domains (seed 1), 128^2..1024^2, circular diaphragms, 400 steps",
         "omp2d": f"2D second-order SHLL with the MC limiter (alpha 1.25), {cells}x{cells}, four-quadrant initial data "
-                 f"of base-omp, t=0.3 (plain FP64 on the GPU)",
+                 f"of base-omp, t=0.3",
     }[workload]
 
 
@@ -413,9 +413,8 @@ def job_value(world, cell_updates_per_run, runs, seconds):
 
 
 DEFAULT_CELLS = {"sod1d": 65536, "circle2d": 4096, "omp2d": 1024}
-# the arithmetic each workload is measured in (the 2D mixed engine is first order: the second-order
-# base-omp problem runs the plain FP64 path)
-PRECISION = {"omp2d": "f64"}
+# the arithmetic each workload is measured in, where it is not --precision
+PRECISION = {}
 
 
 def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, world, rank, local, extras,
@@ -458,7 +457,8 @@ def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, w
     hbm, peak_kind = peaks()
     bytes_per_cu = 64.0 if prob.dim == 2 else 48.0
     kernel = {"sod1d": "k_tube1d" if launches <= 3 * steps else "k_sweep1d", "batch1d": "k_sweep1d",
-              "circle2d": "k_step2d", "batch2d": "k_step2d", "omp2d": "k_step2"}[workload]
+              "circle2d": "k_step2d", "batch2d": "k_step2d",
+              "omp2d": "k_step2d_o2" if precision.startswith("mixed") else "k_step2"}[workload]
     achieved = bytes_per_cu * prob.cu * steps / t_total / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": profile_traffic(kernel, workload), "peak_kind": peak_kind, "kernel": kernel,
@@ -497,7 +497,7 @@ def measure(shll, torch, stream, workload, cells, order, args, steps, W, dist, w
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if extras and rank == 0 and workload == "omp2d":
+    if extras and rank == 0 and not precision.startswith("mixed"):
         out["cpu_baseline"] = cpu_baseline(workload, cells, order)
     elif extras and rank == 0:
         out.update(fp64_comparison(shll, torch, stream, prob, args, cells, order, mixed_out, t_total / steps))
@@ -772,6 +772,15 @@ def fp64_comparison(shll, torch, stream, prob, args, cells, order, mixed_out, t_
                          "precision": prec64}
     out["speedup_vs_fp64_plain"] = (prob.cu / t_run) / (prob.cu / t64)
     out["l1_vs_fp64"] = dict(zip(names, [float(x) for x in l1]))
+    if prec64 == "f64":
+        # how far the FP64 result is reproducible at all: the same run without fused multiply-add
+        ctx = shll.Context(params_single(shll, prob.workload, "f64_exact", cells, order, 0))
+        ctx.set_stream(stream.cuda_stream)
+        ctx.init_state()
+        ctx.run()
+        floor = np.mean(np.abs(ctx.primitives() - f64_out), axis=1)
+        ctx.close()
+        out["l1_fp64_fma_vs_exact"] = dict(zip(names, [float(x) for x in floor]))
     if prob.workload == "sod1d":
         O = oracle_mod()
         ex = O.riemann_exact(cells, shll.steps_for(prob.p) * (0.125 / cells))

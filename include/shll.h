@@ -170,7 +170,9 @@ typedef struct shll_batch shll_batch;
 /* items: count parameter sets (all dim 1, or all dim 2, any sizes/orders/initial data), all
  * with one precision: SHLL_PREC_F64 or SHLL_PREC_F64_EXACT (the plain FP64 arithmetic, with or
  * without fused multiply-add, one launch per time step over every item) or a MIXED mode (the
- * sweep engine in 1D; first order only in 2D).  SHLL_PREC_F32_EXACT batches: SHLL_ERR_UNSUPPORTED. */
+ * sweep engine in 1D; in 2D one step launch per time step over every tile of every domain, first
+ * or second order, with one order and, for second order, one limiter for all items of the batch:
+ * SHLL_ERR_ARG otherwise).  SHLL_PREC_F32_EXACT batches: SHLL_ERR_UNSUPPORTED. */
 int shll_batch_create(const shll_params* items, int count, shll_batch** out);
 /* Runs every item to its own end (its own DT and step count). */
 int shll_batch_run(shll_batch* b);

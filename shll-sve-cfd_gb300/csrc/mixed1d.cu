@@ -607,7 +607,7 @@ __device__ void sweep_chunk(const SweepArgs& A, const int sweep, const Chunk& ch
                 ol = add2(fma2(lout2, OUT, neg2(oh)), mul2(llout2, OUT));
             }
             two_sum_acc2(dh[k], dl[k], ih);
-            two_sum_acc2(dh[k], dl[k], neg2(oh));
+            two_diff_acc2(dh[k], dl[k], oh);
             if (!LAM_POW2) dl[k] = add2(dl[k], sub2(il, ol));
             ihk[k] = ih; ohk[k] = oh; ilk[k] = il; olk[k] = ol;
         }

@@ -63,6 +63,7 @@ struct Dom2 {
     int steps;                // steps of the current run
     double gamma, R, CV, lamx, lamy;
     float lxh, lxl, lyh, lyl; // lam_x, lam_y as FP32 pairs
+    float alpha;              // MC limiter coefficient (second order, limiter 1)
 };
 
 struct TileD { int dom, ti, tj; };
@@ -375,6 +376,7 @@ __global__ void __launch_bounds__(64) k_tileconst2d(Args2 A) {
 // (j0-2, j0-1) and north (j0+32, j0+33)).  Every thread evaluates one pair's split fluxes, then,
 // after the one barrier, each owner thread sums its pair's four interfaces per component.
 constexpr int NTP = 320;
+static_assert(kTileC2Words <= NTP, "the tile constants are copied one word per thread");
 constexpr int WR = TI + 2;        // window rows (i0-1 .. i0+TI)
 constexpr int WP = TJ / 2 + 2;    // window pairs per row (cells j0-2 .. j0+TJ+1)
 
@@ -436,14 +438,17 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
                 if (cjq < 0 || cjq >= D.ny) continue;    // outside the domain: zero deviation
                 const int cell = D.base + ci * D.ny + cjq;
                 float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
-                if (kw > 0 && on_edge_line(ci, cjq)) edge_correction(A, D, ci, cjq, pp, ch, cl);
+                const bool edge = kw > 0 && on_edge_line(ci, cjq);
+                if (edge) edge_correction(A, D, ci, cjq, pp, ch, cl);
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const int idx = k * P + cell;
                     float h = 0.f, l = 0.f;
                     if (kw > 0) { h = phi[idx]; l = pli[idx]; }
-                    two_sum_acc(h, l, ch[k]);   // the pending edge correction joins the increment pair
-                    l = __fadd_rn(l, cl[k]);
+                    if (edge) {   // the pending edge correction joins the increment pair
+                        two_sum_acc(h, l, ch[k]);
+                        l = __fadd_rn(l, cl[k]);
+                    }
                     if (nb < 0) { set_lane(Ph[k], q, h); set_lane(Pl[k], q, l); }
                     // deviation from this tile's frame: C (relative to the owner's frame) + the
                     // owner's frame offset + the increments
@@ -489,6 +494,10 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
             two_sum_acc2(ah, al, th);
             if (!LAM_POW2) al = add2(al, tl);
         };
+        auto dec = [&](float2 th, float2 tl) {   // (ah, al) -= (th, tl)
+            two_diff_acc2(ah, al, th);
+            if (!LAM_POW2) al = sub2(al, tl);
+        };
         float2 th, tl;
         // x west
         if (i > 0) {
@@ -507,7 +516,7 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
         // x east
         if (i < D.nx - 1) {
             lam(lx2, lxl2, add2(fp, S.f[4 + k][r + 1][c]), th, tl);
-            acc(neg2(th), neg2(tl));
+            dec(th, tl);
             if (r == hi_i) {
                 Edge* e = exo + D.ex_base + ((i + 1) / TI - 1) * D.ny + jx;
                 ff_add(S.lf[0][k][0], S.lf[0][k][1], th.x, tl.x, e[0].r[0][k][0], e[0].r[0][k][1]);
@@ -534,7 +543,7 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
             const float hmN = S.f[12 + k][r][c + 1].x;
             lam(ly2, lyl2, add2(hp, make_float2(hm.y, hmN)), th, tl);
             th = mul2(th, mN); tl = mul2(tl, mN);
-            acc(neg2(th), neg2(tl));
+            dec(th, tl);
             const int jn = j0 + hi_j - 1;   // the tile's north edge column
             if (jn + 1 < D.ny && (jx == jn || jx + 1 == jn)) {
                 const int q = jx == jn ? 0 : 1;
@@ -647,14 +656,17 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
         if (!ex[q]) continue;   // outside the domain: zero deviation (finite fluxes, never applied)
         const int cell = D.base + i * D.ny + jx + q;
         float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
-        if (kw > 0 && on_edge_line(i, jx + q)) edge_correction(A, D, i, jx + q, pp, ch, cl);
+        const bool edge = kw > 0 && on_edge_line(i, jx + q);
+        if (edge) edge_correction(A, D, i, jx + q, pp, ch, cl);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int idx = k * P + cell;
             float h = 0.f, l = 0.f;
             if (kw > 0) { h = phi[idx]; l = pli[idx]; }
-            two_sum_acc(h, l, ch[k]);   // the pending edge correction joins the increment pair
-            l = __fadd_rn(l, cl[k]);
+            if (edge) {   // the pending edge correction joins the increment pair
+                two_sum_acc(h, l, ch[k]);
+                l = __fadd_rn(l, cl[k]);
+            }
             set_lane(ah[k], q, h);
             set_lane(al[k], q, l);
             // deviation from this tile's frame: C (relative to the owner's frame) + the owner's frame offset
@@ -716,6 +728,10 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
                 two_sum_acc2(h2, l2, th);
                 if (!LAM_POW2) l2 = add2(l2, tl);
             };
+            auto dec = [&](float2 th, float2 tl) {
+                two_diff_acc2(h2, l2, th);
+                if (!LAM_POW2) l2 = sub2(l2, tl);
+            };
             float2 th, tl;
             // x west
             if (i > 0) {
@@ -732,7 +748,7 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
             // x east
             if (i < D.nx - 1) {
                 lam(lx2, lxl2, add2(fp, flux(b, 4 + k, wr + 1, wc)), th, tl);
-                acc(neg2(th), neg2(tl));
+                dec(th, tl);
                 if (recE)
                     for (int q = 0; q < 2; q++)
                         if (rec[q]) record(S.recx[1][jx + q - j0][k], lane(th, q), lane(tl, q));
@@ -752,7 +768,7 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
             {
                 lam(ly2, lyl2, add2(hp, make_float2(hm.y, flux(b, 12 + k, wr, cn).x)), th, tl);
                 th = mul2(th, mN); tl = mul2(tl, mN);
-                acc(neg2(th), neg2(tl));
+                dec(th, tl);
                 for (int q = 0; q < 2; q++)
                     if (rec[q] && jx + q == j0 + hi_j - 1 && jx + q + 1 < D.ny)
                         record(S.recy[1][wr - 2][k], lane(th, q), lane(tl, q));
@@ -823,6 +839,201 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
     }
 }
 
+// ---- one second-order time step of one tile ----
+// The x and y sweeps of base-c/2nd_order_base_shll.c:203-459 (and the MC limiter of
+// base-omp/2nd_order_base_shll.c:316-325) as interface fluxes: with the face values
+// Lx_i = fp_i + sp_i/2 and Rx_i = fm_i - sm_i/2 (sp, sm the limited slopes of the split fluxes,
+// zero on the domain's edge cells), F_{i+1/2} = Lx_i + Rx_{i+1}, and the cell gains
+// lam_x (F_{i-1/2} - F_{i+1/2}) + lam_y (H_{j-1/2} - H_{j+1/2}).  At an outflow wall the wall flux is
+// the wall cell's own Lx + Rx = fp + fm (2nd_order_base_shll.c:236-262), so the frame's reference
+// flux cancels from every increment and the walls need no constant terms.
+// The window is the tile and two cells on each side (20 rows x 18 pairs; the corner pairs are not
+// needed), one thread per pair.  Phase 1: split-flux deviations of every window pair in this
+// tile's frame.  Phase 2: face values, x for the rows i0-1 .. i0+16 of the tile's columns, y for the
+// tile's rows and the columns j0-1 .. j0+32.  Phase 3: the own pairs' four interfaces, TwoSum into
+// their increment pairs, and the tile's edge records (as in the first-order kernel).
+constexpr int kStepO2Smem = 2 * 16 * WR2 * WP * (int)sizeof(float2);   // split fluxes, face values
+
+struct SmemO2 {             // the tile's step constants (a copy of its TileC2)
+    float wc[4][4][2];
+    float lf[2][4][2];
+    float dn[4][4][2];
+    float dnd[4][4][2];
+    Coef2D cf;
+};
+static_assert(sizeof(SmemO2) == sizeof(TileC2), "the tile constants are copied word for word");
+
+template <bool KAHAN, bool LAM_POW2, int LIM>
+__global__ void __launch_bounds__(NT2, 2) k_step2d_o2(Args2 A) {
+    __shared__ SmemO2 S;
+    extern __shared__ __align__(16) float2 g_o2[];   // [32][WR2][WP]: fp fm hp hm, then Lx Rx Ly Ry
+    const TileD tile = A.tiles[blockIdx.x];
+    const Dom2 D = A.doms[tile.dom];
+    if (A.step >= D.steps) return;
+    const int tid = threadIdx.x;
+    const int kw = A.step - A.s0;                         // step within the fold window
+    const int i0 = tile.ti * TI, j0 = tile.tj * TJ;
+    const int hi_i = min(TI, D.nx - i0), hi_j = min(TJ, D.ny - j0);
+    const int P = A.plane;
+    const int tb = D.tile_base + tile.ti * D.tiles_j + tile.tj;
+    const float* phi = A.Ph[kw % 3];                      // increments so far (kw = 0: none)
+    const float* pli = A.Pl[kw % 3];
+    float* pho = A.Ph[(kw + 1) % 3];
+    float* plo = A.Pl[(kw + 1) % 3];
+    const int pp = (A.step + 2) % 3;                      // edge buffers of the previous step
+    if (tid < kTileC2Words)
+        reinterpret_cast<float*>(&S)[tid] = reinterpret_cast<const float*>(&A.tc[tb])[tid];
+    auto fl = [&](int q, int r, int c) -> float2& { return g_o2[(q * WR2 + r) * WP + c]; };
+
+    // ---- this thread's window pair: row wr (cell row i), pair column wc (cells jx, jx + 1) ----
+    const bool pt = tid < WR2 * WP;
+    const int wr = pt ? tid / WP : 0, wc = pt ? tid % WP : 0;
+    const int i = i0 - 2 + wr, jx = j0 - 2 + 2 * wc;
+    const int di = wr < 2 ? -1 : (wr >= 2 + TI ? 1 : 0), dj = wc == 0 ? -1 : (wc == WP - 1 ? 1 : 0);
+    // owner tile of the pair (-1 this tile, 0 W, 1 E, 2 S, 3 N); corner pairs are left out
+    const int nbi = di == 0 && dj == 0 ? -1 : dj == 0 ? (di < 0 ? 0 : 1) : (dj < 0 ? 2 : 3);
+    bool ex[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+        ex[q] = pt && (di == 0 || dj == 0) && i >= 0 && i < D.nx && jx + q >= 0 && jx + q < D.ny;
+    const bool ro = wr >= 2 && wr < 2 + hi_i;
+    const bool own[2] = {ex[0] && ro && jx >= j0 && jx < j0 + hi_j, ex[1] && ro && jx + 1 >= j0 && jx + 1 < j0 + hi_j};
+    __syncthreads();   // (the tile constants)
+
+    // ---- phase 1: deviations and split fluxes ----
+    float2 ah[4], al[4];   // the pair's increments so far (own pairs)
+    {
+        float2 d[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) { d[k] = f2(0.f); ah[k] = f2(0.f); al[k] = f2(0.f); }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if (!ex[q]) continue;   // outside the domain or a corner: zero deviation (finite, never applied)
+            const int cell = D.base + i * D.ny + jx + q;
+            float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
+            const bool edge = kw > 0 && on_edge_line(i, jx + q);
+            if (edge) edge_correction(A, D, i, jx + q, pp, ch, cl);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int idx = k * P + cell;
+                float h = 0.f, l = 0.f;
+                if (kw > 0) { h = phi[idx]; l = pli[idx]; }
+                if (edge) {   // the pending edge correction joins the increment pair
+                    two_sum_acc(h, l, ch[k]);
+                    l = __fadd_rn(l, cl[k]);
+                }
+                set_lane(ah[k], q, h);
+                set_lane(al[k], q, l);
+                float b = A.C[idx];
+                if (nbi >= 0) b = __fadd_rn(__fadd_rn(b, S.dn[nbi][k][0]), S.dn[nbi][k][1]);
+                set_lane(d[k], q, __fadd_rn(b, __fadd_rn(h, l)));
+            }
+        }
+        float2 fp[4], fm[4], hp[4], hm[4];
+        dflux2x2(S.cf, d, fp, fm, hp, hm);
+        if (pt) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                fl(k, wr, wc) = fp[k]; fl(4 + k, wr, wc) = fm[k];
+                fl(8 + k, wr, wc) = hp[k]; fl(12 + k, wr, wc) = hm[k];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase 2: face values ----
+    const float alpha = D.alpha;
+    if (pt && wr >= 1 && wr <= TI + 2 && wc >= 1 && wc <= TJ / 2) {
+        // x: slopes along i, zero on the edge cells i = 0, nx - 1 (and outside the domain)
+        const float hx = (i <= 0 || i >= D.nx - 1) ? 0.f : 0.5f;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float2 pm = fl(k, wr - 1, wc), pc = fl(k, wr, wc), pq = fl(k, wr + 1, wc);
+            fl(16 + k, wr, wc) = fma2(f2(hx), slope2<LIM>(sub2(pc, pm), sub2(pq, pc), alpha), pc);
+            const float2 mm = fl(4 + k, wr - 1, wc), mc = fl(4 + k, wr, wc), mq = fl(4 + k, wr + 1, wc);
+            fl(20 + k, wr, wc) = fma2(f2(-hx), slope2<LIM>(sub2(mc, mm), sub2(mq, mc), alpha), mc);
+        }
+    }
+    if (pt && wr >= 2 && wr < 2 + TI) {
+        // y: slopes along j (lane x needs the south pair's lane y, lane y the north pair's lane x;
+        // the clamped neighbours only serve lanes that no interface reads), zero on j = 0, ny - 1
+        const int cs = max(wc - 1, 0), cn = min(wc + 1, WP - 1);
+        const float2 hy = make_float2((jx <= 0 || jx >= D.ny - 1) ? 0.f : 0.5f,
+                                      (jx + 1 <= 0 || jx + 1 >= D.ny - 1) ? 0.f : 0.5f);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float2 pc = fl(8 + k, wr, wc);
+            const float2 pb = make_float2(fl(8 + k, wr, cs).y, pc.x), pn = make_float2(pc.y, fl(8 + k, wr, cn).x);
+            fl(24 + k, wr, wc) = fma2(hy, slope2<LIM>(sub2(pc, pb), sub2(pn, pc), alpha), pc);
+            const float2 mc = fl(12 + k, wr, wc);
+            const float2 mb = make_float2(fl(12 + k, wr, cs).y, mc.x), mn = make_float2(mc.y, fl(12 + k, wr, cn).x);
+            fl(28 + k, wr, wc) = fma2(neg2(hy), slope2<LIM>(sub2(mc, mb), sub2(mn, mc), alpha), mc);
+        }
+    }
+    __syncthreads();
+    if (!(own[0] || own[1])) return;
+
+    // ---- phase 3: interfaces and increments of the own pair ----
+    const bool has_y = own[1];
+    const float2 lx2 = f2(D.lxh), lxl2 = f2(D.lxl), ly2 = f2(D.lyh), lyl2 = f2(D.lyl);
+    const bool wW = i == 0, wE = i == D.nx - 1;                       // x walls (whole pair)
+    const bool wS = jx == 0, wNx = jx == D.ny - 1, wNy = jx + 1 == D.ny - 1;   // y walls per lane
+    const bool recW = wr == 2 && i0 > 0, recE = wr == 2 + hi_i - 1 && i + 1 < D.nx;
+    const int jn = j0 + hi_j - 1;   // the tile's north edge column
+    const bool recN = jn + 1 < D.ny && (jx == jn || jx + 1 == jn);
+    const int qn = jx == jn ? 0 : 1;
+    Edge* exo = A.ex[A.step % 3];
+    Edge* eyo = A.ey[A.step % 3];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float2 Lx = fl(16 + k, wr, wc), Rx = fl(20 + k, wr, wc);
+        const float2 Ly = fl(24 + k, wr, wc), Ry = fl(28 + k, wr, wc);
+        float2 h = ah[k], l = al[k];
+        auto lam = [&](float2 lh, float2 ll, float2 x, float2& th, float2& tl) {
+            th = mul2(lh, x);
+            tl = LAM_POW2 ? f2(0.f) : add2(fma2(lh, x, neg2(th)), mul2(ll, x));
+        };
+        float2 th, tl;
+        // x west: F_{i-1/2} = Lx_{i-1} + Rx_i (wall: the cell's own Lx + Rx)
+        lam(lx2, lxl2, add2(wW ? Lx : fl(16 + k, wr - 1, wc), Rx), th, tl);
+        two_sum_acc2(h, l, th);
+        if (!LAM_POW2) l = add2(l, tl);
+        if (recW) {   // the tile's west edge: record the full flux this tile applied
+            Edge* e = exo + D.ex_base + (i / TI - 1) * D.ny + jx;
+            ff_add(S.lf[0][k][0], S.lf[0][k][1], th.x, tl.x, e[0].r[1][k][0], e[0].r[1][k][1]);
+            if (has_y) ff_add(S.lf[0][k][0], S.lf[0][k][1], th.y, tl.y, e[1].r[1][k][0], e[1].r[1][k][1]);
+        }
+        // x east: F_{i+1/2} = Lx_i + Rx_{i+1}
+        lam(lx2, lxl2, add2(Lx, wE ? Rx : fl(20 + k, wr + 1, wc)), th, tl);
+        two_diff_acc2(h, l, th);
+        if (!LAM_POW2) l = sub2(l, tl);
+        if (recE) {
+            Edge* e = exo + D.ex_base + ((i + 1) / TI - 1) * D.ny + jx;
+            ff_add(S.lf[0][k][0], S.lf[0][k][1], th.x, tl.x, e[0].r[0][k][0], e[0].r[0][k][1]);
+            if (has_y) ff_add(S.lf[0][k][0], S.lf[0][k][1], th.y, tl.y, e[1].r[0][k][0], e[1].r[0][k][1]);
+        }
+        // y south: lanes (jx-1 | jx) and (jx | jx+1); lane x at the south wall: its own Ly + Ry
+        lam(ly2, lyl2, add2(make_float2(wS ? Ly.x : fl(24 + k, wr, wc - 1).y, Ly.x), Ry), th, tl);
+        two_sum_acc2(h, l, th);
+        if (!LAM_POW2) l = add2(l, tl);
+        if (jx == j0 && j0 > 0) {   // the tile's south edge (lane x)
+            float* rr = eyo[D.ey_base + (j0 / TJ - 1) * D.nx + i].r[1][k];
+            ff_add(S.lf[1][k][0], S.lf[1][k][1], th.x, tl.x, rr[0], rr[1]);
+        }
+        // y north: lanes (jx | jx+1) and (jx+1 | jx+2); at the north wall the lane's own Ly + Ry
+        lam(ly2, lyl2, add2(Ly, make_float2(wNx ? Ry.x : Ry.y, wNy ? Ry.y : fl(28 + k, wr, min(wc + 1, WP - 1)).x)), th, tl);
+        two_diff_acc2(h, l, th);
+        if (!LAM_POW2) l = sub2(l, tl);
+        if (recN) {
+            float* rr = eyo[D.ey_base + ((jn + 1) / TJ - 1) * D.nx + i].r[0][k];
+            ff_add(S.lf[1][k][0], S.lf[1][k][1], lane(th, qn), lane(tl, qn), rr[0], rr[1]);
+        }
+        const int cell = D.base + i * D.ny + jx;
+        if (own[0]) { pho[k * P + cell] = h.x; plo[k * P + cell] = l.x; }
+        if (has_y) { pho[k * P + cell + 1] = h.y; plo[k * P + cell + 1] = l.y; }
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
@@ -849,6 +1060,7 @@ struct Mixed2D {
     Dom2* d_doms = nullptr;
     TileD* d_tiles = nullptr;
     int fold = 16;
+    int order = 1, lim = 0;        // the batch's scheme (second order: minmod 0 or MC 1)
     int kstep = default_kstep();   // time steps per step launch (k_step2d2 for 2, k_step2d for 1)
     // device checkpoint of the stored state (a run starts with a fold that rebuilds frames, C and
     // the tile constants from it, so the stored state is the whole state between runs)
@@ -861,17 +1073,17 @@ struct Mixed2D {
     std::vector<std::pair<std::vector<int>, int>> seen;   // (step counts, fold * 4 + kstep)
 };
 
-// fold windows chosen by the autotuner, process-wide, by (state format, floor(log2 of the largest
-// domain's cells)); applied to later 2D batches whose items leave fold_steps at 0
+// fold windows chosen by the autotuner, process-wide, by (state format and scheme, floor(log2 of the
+// largest domain's cells)); applied to later 2D batches whose items leave fold_steps at 0
 static std::mutex g_tune2d_mu;
 static std::map<std::pair<int, int>, std::pair<int, int>> g_tune2d;   // -> (fold window, steps per launch)
 
-static std::pair<int, int> tune2d_key(const std::vector<Dom2>& doms, bool kahan) {
+static std::pair<int, int> tune2d_key(const std::vector<Dom2>& doms, bool kahan, int order, int lim) {
     long cells = 1;
     for (const Dom2& D : doms) cells = std::max(cells, (long)D.nx * D.ny);
     int lg = 0;
     while ((2L << lg) <= cells) lg++;
-    return {kahan ? 1 : 0, lg};
+    return {(kahan ? 1 : 0) + 2 * (order == 2 ? 1 + lim : 0), lg};
 }
 
 static Mixed2D* get2(MixedState* m) { return static_cast<Mixed2D*>(*mixed_d2_slot(m)); }
@@ -881,13 +1093,17 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
     int count = 0;
     const shll_params* items = mixed_items(m, &count);
     for (int t = 0; t < count; t++) {
-        if (items[t].order != 1) {
-            snprintf(err, len, "2D mixed precision supports first order only (item %d)", t);
+        // one scheme per batch: the step kernel is specialised on the order and the limiter
+        if (items[t].order != items[0].order || (items[0].order == 2 && items[t].limiter != items[0].limiter)) {
+            snprintf(err, len, "2D mixed precision: every domain of a batch needs the same order and limiter (item %d)", t);
             return nullptr;
         }
     }
     Mixed2D* d = new Mixed2D();
     *mixed_d2_slot(m) = d;
+    d->order = items[0].order;
+    d->lim = d->order == 2 && items[0].limiter == 1 ? 1 : 0;
+    if (d->order == 2) d->kstep = 1;   // (the two-step kernel is first order)
     d->fold = std::max(1, mixed_fold(m));
     long off = 0, oex = 0, oey = 0, otile = 0;
     for (int t = 0; t < count; t++) {
@@ -911,6 +1127,7 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
         D.lamy = dt / dy;
         D.lxh = (float)D.lamx; D.lxl = (float)(D.lamx - (double)D.lxh);
         D.lyh = (float)D.lamy; D.lyl = (float)(D.lamy - (double)D.lyh);
+        D.alpha = (float)p.mc_alpha;
         d->doms.push_back(D);
         for (int a = 0; a < D.tiles_i; a++)
             for (int b = 0; b < D.tiles_j; b++) d->tiles.push_back({t, a, b});
@@ -927,8 +1144,8 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
     }
     if (items[0].fold_steps <= 0) {   // a tuned fold window of this class
         std::lock_guard<std::mutex> lk(g_tune2d_mu);
-        auto it = g_tune2d.find(tune2d_key(d->doms, mixed_is_kahan(m)));
-        if (it != g_tune2d.end()) { d->fold = it->second.first; d->kstep = it->second.second; }
+        auto it = g_tune2d.find(tune2d_key(d->doms, mixed_is_kahan(m), d->order, d->lim));
+        if (it != g_tune2d.end()) { d->fold = it->second.first; if (d->order == 1) d->kstep = it->second.second; }
     }
     d->plane = off;
     d->nex = std::max(oex, 1L);
@@ -988,8 +1205,22 @@ int mixed2d_planes(MixedState* m, int item, MixedPlanes* out) {
     return SHLL_OK;
 }
 
-// the launches of one run on stream s: the opening fold, then per step k_step2d and a fold at the
-// end of every window
+// the second-order step kernel of the batch's variant
+static void launch_o2(bool kahan, bool pow2, int lim, int ntiles, cudaStream_t s, const Args2& A) {
+    switch ((kahan ? 4 : 0) + (pow2 ? 2 : 0) + lim) {
+        case 0: k_step2d_o2<false, false, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 1: k_step2d_o2<false, false, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 2: k_step2d_o2<false, true, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 3: k_step2d_o2<false, true, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 4: k_step2d_o2<true, false, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 5: k_step2d_o2<true, false, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 6: k_step2d_o2<true, true, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        default: k_step2d_o2<true, true, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+    }
+}
+
+// the launches of one run on stream s: the opening fold, then per step k_step2d (k_step2d2 for two
+// steps, k_step2d_o2 for second order) and a fold at the end of every window
 static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s) {
     Args2 A;
     memset(&A, 0, sizeof(A));
@@ -1030,7 +1261,9 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
         // two steps per launch inside a fold window, one for an odd remainder
         const long wend = std::min<long>(s0 + d->fold, maxsteps);
         const int k = d->kstep == 2 && wend - st >= 2 ? 2 : 1;
-        if (k == 2) {
+        if (d->order == 2) {
+            launch_o2(kahan, pow2, d->lim, ntiles, s, A);
+        } else if (k == 2) {
             if (kahan) {
                 if (pow2) k_step2d2<true, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
                 else k_step2d2<true, false><<<ntiles, NT2, kStep2Smem, s>>>(A);
@@ -1055,7 +1288,8 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
     return launches;
 }
 
-// allows the two-step kernel its dynamic shared memory on the current device (before any capture)
+// allows the two-step and second-order kernels their dynamic shared memory on the current device
+// (before any capture)
 static cudaError_t allow_step2_smem() {
     static unsigned long long done = 0;
     int dev = 0;
@@ -1065,6 +1299,14 @@ static cudaError_t allow_step2_smem() {
                         (const void*)k_step2d2<true, false>, (const void*)k_step2d2<true, true>};
     for (const void* k : ks) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kStep2Smem);
+        if (e != cudaSuccess) return e;
+    }
+    const void* ko[] = {(const void*)k_step2d_o2<false, false, 0>, (const void*)k_step2d_o2<false, false, 1>,
+                        (const void*)k_step2d_o2<false, true, 0>, (const void*)k_step2d_o2<false, true, 1>,
+                        (const void*)k_step2d_o2<true, false, 0>, (const void*)k_step2d_o2<true, false, 1>,
+                        (const void*)k_step2d_o2<true, true, 0>, (const void*)k_step2d_o2<true, true, 1>};
+    for (const void* k : ko) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kStepO2Smem);
         if (e != cudaSuccess) return e;
     }
     done |= 1ull << dev;
@@ -1190,7 +1432,7 @@ int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
     float best_ms = 1e30f;
     for (int cand = 0; cand < 8; cand++) {
         const int f = 16 << (cand / 2), kk = 1 + cand % 2;
-        if (f > trial_steps) continue;
+        if (f > trial_steps || (kk == 2 && d->order == 2)) continue;
         d->fold = f;
         d->kstep = kk;
         float ms = 1e30f;
@@ -1217,7 +1459,7 @@ int mixed2d_autotune(MixedState* m, int trial_steps, char* err, size_t len) {
     if (rc != SHLL_OK) return rc;
     if (rc2 != SHLL_OK) return rc2;
     std::lock_guard<std::mutex> lk(g_tune2d_mu);
-    g_tune2d[tune2d_key(d->doms, mixed_is_kahan(m))] = {best, bestk};
+    g_tune2d[tune2d_key(d->doms, mixed_is_kahan(m), d->order, d->lim)] = {best, bestk};
     return SHLL_OK;
 }
 

@@ -1,5 +1,6 @@
-"""GPU tests of the 2D mixed-precision engine (first order, reflective walls) against the FP64
-oracle (a restatement of base-c/base_shll_2d.c pinned bit for bit to the reference).
+"""GPU tests of the 2D mixed-precision engine (first order with reflective walls, second order with
+outflow walls) against the FP64 oracle (a restatement of base-c/base_shll_2d.c and
+base-c/2nd_order_base_shll.c pinned bit for bit to the reference).
 
 Tolerances: L1(rho, u, v, T) <= 1e-6 against the FP64 oracle; mass and energy conserved to
 <= 1e-12 relative (reflective walls)."""
@@ -81,10 +82,74 @@ def test_batch_of_domains(shll, oracle):
         assert np.all(l1(b.primitives(k), refs[k]) <= 1e-6), k
 
 
-def test_second_order_2d_mixed_is_refused(shll):
-    with pytest.raises(shll.ShllError) as e:
-        shll.Context(shll.params(2, 2, nx=32, ny=32, precision="mixed_f64"))
-    assert e.value.status == shll.ERR_NOMEM or e.value.status == shll.ERR_UNSUPPORTED
+# ---- second order (base-c/2nd_order_base_shll.c:203-459 in x and y, outflow walls; the MC limiter
+# of base-omp/2nd_order_base_shll.c:316-325) ----
+
+@pytest.mark.parametrize("prec", ["mixed_f64", "mixed_kahan"])
+@pytest.mark.parametrize("limiter,ic", [(0, "four_shock"), (1, "quadrants")])
+@pytest.mark.parametrize("nx,ny,steps", [(16, 32, 40), (40, 70, 120), (64, 64, 200), (100, 37, 90), (2, 5, 20),
+                                         (33, 65, 60)])
+def test_second_order_vs_fp64_oracle(shll, oracle, prec, limiter, ic, nx, ny, steps):
+    cfg = oracle.make_cfg(dim=2, order=2, nx=nx, ny=ny, n_steps=steps, limiter=limiter, mc_alpha=1.25)
+    prim = oracle.ic_four_shock2d(nx, ny, 64) if ic == "four_shock" else oracle.ic_quadrants2d(nx, ny, 64)
+    _, ref, _ = oracle.run(cfg, prim)
+    kind = shll.IC_FOUR_SHOCK2D if ic == "four_shock" else shll.IC_QUADRANTS2D
+    p = shll.params(2, 2, nx=nx, ny=ny, precision=prec, n_steps=steps, limiter=limiter, mc_alpha=1.25, ic_kind=kind)
+    s, out, _, _ = run(shll, p)
+    assert s == steps
+    err = l1(out, ref)
+    assert np.all(err <= 1e-6), err
+
+
+def test_second_order_conserves_away_from_the_walls(shll, oracle):
+    # a diaphragm well inside the domain: no wave reaches the outflow walls within 8 steps (two cells
+    # of reach per step), so mass, momentum and energy are conserved to the rounding of the state
+    n, steps = 64, 8
+    p = shll.params(2, 2, nx=n, ny=n, precision="mixed_f64", n_steps=steps, ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5,
+                    ic_cy=0.5, ic_radius=0.15, ic_rho_l=20.0, ic_T_l=1.5, ic_rho_r=1.0, ic_T_r=1.0)
+    _, out, t0, t1 = run(shll, p)
+    cfg = oracle.make_cfg(dim=2, order=2, nx=n, ny=n, n_steps=steps)
+    _, ref, _ = oracle.run(cfg, oracle.ic_circle2d(n, n, r=0.15, rho_in=20.0, T_in=1.5))
+    assert np.all(l1(out, ref) <= 1e-6)
+    assert abs(t1[0] - t0[0]) / t0[0] <= 1e-12
+    assert abs(t1[3] - t0[3]) / t0[3] <= 1e-12
+
+
+def test_second_order_batch_and_replay(shll, oracle):
+    # several second-order domains of different sizes in one batch, run twice from a checkpoint (the
+    # second run replays a captured graph): each equals its single-domain oracle run
+    rng = np.random.default_rng(11)
+    items, refs = [], []
+    for k in range(5):
+        n = int(rng.choice([20, 33, 48, 64]))
+        r = float(rng.uniform(0.1, 0.3))
+        rin = float(rng.uniform(2, 20))
+        steps = int(rng.integers(10, 50))
+        items.append(shll.params(2, 2, nx=n, ny=n, precision="mixed_f64", n_steps=steps, ic_kind=shll.IC_CIRCLE2D,
+                                 ic_cx=0.5, ic_cy=0.5, ic_radius=r, ic_rho_l=rin, ic_T_l=1.0, ic_rho_r=1.0,
+                                 ic_T_r=1.0))
+        cfg = oracle.make_cfg(dim=2, order=2, nx=n, ny=n, n_steps=steps)
+        refs.append(oracle.run(cfg, oracle.ic_circle2d(n, n, r=r, rho_in=rin))[1])
+    import torch
+    st = torch.cuda.Stream()
+    b = shll.Batch(items)
+    b.set_stream(st.cuda_stream)
+    b.checkpoint()
+    outs = []
+    for _ in range(3):
+        b.restore()
+        b.run()
+        outs.append([b.primitives(k) for k in range(len(items))])
+    b.close()
+    for k in range(len(items)):
+        assert np.all(l1(outs[0][k], refs[k]) <= 1e-6), k
+        assert np.array_equal(outs[0][k], outs[2][k])
+
+
+def test_second_order_batch_needs_one_limiter(shll):
+    items = [shll.params(2, 2, nx=32, ny=32, precision="mixed_f64", limiter=lim, mc_alpha=1.25) for lim in (0, 1)]
+    with pytest.raises(shll.ShllError):
+        shll.Batch(items)
 
 
 def test_checkpoint_restore_and_graph_replay(shll):
