@@ -167,15 +167,24 @@ def items_batch2d(shll, precision, count=256, seed=1, fold=0):
     return out
 
 
+# --run-steps: a fixed step count for the single-domain workloads (short runs of the same kernels,
+# for profiling); 0 keeps each workload's own end time or step count
+RUN_STEPS = 0
+
+
 def params_single(shll, workload, precision, cells, order, fold):
     if workload == "omp2d":   # base-omp/2nd_order_base_shll.c:30-44, 147-172 (MC limiter, "Configuration 6")
-        return shll.params(2, 2, nx=cells, ny=cells, precision=precision, t_end=0.3, limiter=1, mc_alpha=1.25,
-                           ic_kind=shll.IC_QUADRANTS2D)
-    if workload == "sod1d":
-        return shll.params(1, order, nx=cells, precision=precision, t_end=0.2, fold_steps=fold)
-    return shll.params(2, 1, nx=cells, ny=cells, precision=precision, n_steps=500, fold_steps=fold,
-                       ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5, ic_cy=0.5, ic_radius=0.25, ic_rho_l=10.0,
-                       ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0)
+        p = shll.params(2, 2, nx=cells, ny=cells, precision=precision, t_end=0.3, limiter=1, mc_alpha=1.25,
+                        ic_kind=shll.IC_QUADRANTS2D, fold_steps=fold)
+    elif workload == "sod1d":
+        p = shll.params(1, order, nx=cells, precision=precision, t_end=0.2, fold_steps=fold)
+    else:
+        p = shll.params(2, 1, nx=cells, ny=cells, precision=precision, n_steps=500, fold_steps=fold,
+                        ic_kind=shll.IC_CIRCLE2D, ic_cx=0.5, ic_cy=0.5, ic_radius=0.25, ic_rho_l=10.0,
+                        ic_T_l=1.0, ic_rho_r=1.0, ic_T_r=1.0)
+    if RUN_STEPS > 0:
+        p.n_steps = RUN_STEPS
+    return p
 
 
 def describe(workload, cells, order):
@@ -522,7 +531,11 @@ def main():
                     help="measure only --workload (by default the sod1d line also carries batch1d, circle2d "
                          "and batch2d under 'workloads')")
     ap.add_argument("--other-steps", type=int, default=3, help="timed runs of each other workload")
+    ap.add_argument("--run-steps", type=int, default=0,
+                    help="single-domain workloads: a fixed number of time steps per run (small profiling cases)")
     args = ap.parse_args()
+    global RUN_STEPS
+    RUN_STEPS = args.run_steps
     workload = args.workload
     if args.cells == 0:
         args.cells = DEFAULT_CELLS.get(workload, 0)
