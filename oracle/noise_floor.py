@@ -9,7 +9,7 @@ base-c/2nd_order_base_shll.c:191-201, 438-446) amplifies such perturbations stro
 spread grows with the tube size; the first-order scheme on a Sod tube damps them.
 
 spread_stepwise repeats the perturbation every few steps, as an arithmetic that rounds at FP32
-scale in every step does.
+scale in every step does; spread2d measures base-omp's 2D second-order problem.
 
 Command line: python oracle/noise_floor.py [order] [cells ...]
 (e.g. "python oracle/noise_floor.py 2 4096 16384 65536"; 65536 cells take a few minutes per run.)
@@ -57,6 +57,20 @@ def spread_stepwise(n, order=2, x_d=0.5, rhoL=10.0, TL=1.0, eps=6e-8, every=10, 
         done += k
         p = perturbed(p, eps, int(r.integers(1 << 30)))
     return np.mean(np.abs(p - ref), axis=1)
+
+
+def spread2d(n, eps=6e-8, seed=0):
+    """The same distance for base-omp's 2D second-order problem (the quadrant initial data of
+    base-omp/2nd_order_base_shll.c:147-172, MC limiter, t = 0.3) on n x n cells."""
+    cfg = O.make_cfg(dim=2, order=2, nx=n, ny=n, real_bits=64, t_end=0.3, limiter=1, mc_alpha=1.25)
+    prim = O.ic_quadrants2d(n, n, 64)
+    r = np.random.default_rng(seed)
+    pert = prim.copy()
+    pert[0] *= 1.0 + eps * r.uniform(-1.0, 1.0, prim.shape[1])
+    pert[3] *= 1.0 + eps * r.uniform(-1.0, 1.0, prim.shape[1])
+    with concurrent.futures.ThreadPoolExecutor(2) as ex:
+        a, b = ex.map(lambda p: O.run(cfg, p)[1], [prim, pert])
+    return np.mean(np.abs(a - b), axis=1)
 
 
 if __name__ == "__main__":

@@ -256,6 +256,43 @@ __device__ __forceinline__ void edge_correction(const Args2& A, const Dom2& D, i
 
 __device__ __forceinline__ bool on_edge_line(int i, int j) { return (i > 0 && i % TI == 0) || (j > 0 && j % TJ == 0); }
 
+// The increments so far (with the pending edge corrections of the previous step, pp) and C of the
+// cell pair (i, jx), (i, jx + 1), with 8-byte loads: jx even and every domain of the batch with an
+// even row length, so that the pair's index is even and the pair lies wholly inside or outside the
+// domain (the caller checks inside).  Lane by lane the same arithmetic as the per-cell loads.
+__device__ __forceinline__ void load_pair2(const Args2& A, const Dom2& D, int i, int jx, int kw, int pp,
+                                           const float* phi, const float* pli, float2 h[4], float2 l[4],
+                                           float2 c[4]) {
+    const int cell = D.base + i * D.ny + jx;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int idx = k * A.plane + cell;
+        h[k] = f2(0.f);
+        l[k] = f2(0.f);
+        if (kw > 0) {
+            h[k] = *reinterpret_cast<const float2*>(phi + idx);
+            l[k] = *reinterpret_cast<const float2*>(pli + idx);
+        }
+        c[k] = *reinterpret_cast<const float2*>(A.C + idx);
+    }
+    if (kw > 0) {
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if (!on_edge_line(i, jx + q)) continue;
+            float ch[4], cl[4];
+            edge_correction(A, D, i, jx + q, pp, ch, cl);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {   // the pending edge correction joins the increment pair
+                float hh = lane(h[k], q), ll = lane(l[k], q);
+                two_sum_acc(hh, ll, ch[k]);
+                ll = __fadd_rn(ll, cl[k]);
+                set_lane(h[k], q, hh);
+                set_lane(l[k], q, ll);
+            }
+        }
+    }
+}
+
 // (th, tl) = lam * x as an FP32 pair (exact, tl = 0, when lam is an FP32 power of two: POW2)
 template <bool POW2 = false>
 __device__ __forceinline__ void lam_mul(float lh, float ll, float x, float& th, float& tl) {
@@ -389,7 +426,9 @@ struct Smem2 {
     Coef2D cf;
 };
 
-template <bool KAHAN, bool LAM_POW2>
+// VEC: every domain of the batch has an even row length; the pairs are loaded and stored with
+// 8-byte accesses (load_pair2)
+template <bool KAHAN, bool LAM_POW2, bool VEC>
 __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
     __shared__ Smem2 S;
     const TileD tile = A.tiles[blockIdx.x];
@@ -431,7 +470,19 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
         float2 fp[4], fm[4], hp[4], hm[4];
         float2 d[4];
         for (int k = 0; k < 4; k++) { d[k] = f2(0.f); Ph[k] = f2(0.f); Pl[k] = f2(0.f); }
-        if (act) {
+        if (act && VEC) {
+            if (cj >= 0 && cj < D.ny) {                  // (outside the domain: zero deviation)
+                float2 h2[4], l2[4], c2[4];
+                load_pair2(A, D, ci, cj, kw, pp, phi, pli, h2, l2, c2);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (nb < 0) { Ph[k] = h2[k]; Pl[k] = l2[k]; }
+                    float2 base = c2[k];
+                    if (nb >= 0) base = add2(add2(base, f2(S.dn[nb][k][0])), f2(S.dn[nb][k][1]));
+                    d[k] = add2(base, add2(h2[k], l2[k]));
+                }
+            }
+        } else if (act) {
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const int cjq = cj + q;
@@ -570,11 +621,16 @@ __global__ void __launch_bounds__(NTP, 3) k_step2d(Args2 A) {
             }
         }
         const int cell = D.base + i * D.ny + jx;
-        pho[k * P + cell] = ah.x;
-        plo[k * P + cell] = al.x;
-        if (has_y) {
-            pho[k * P + cell + 1] = ah.y;
-            plo[k * P + cell + 1] = al.y;
+        if (VEC) {   // (an even row length: both lanes are own cells)
+            *reinterpret_cast<float2*>(pho + k * P + cell) = ah;
+            *reinterpret_cast<float2*>(plo + k * P + cell) = al;
+        } else {
+            pho[k * P + cell] = ah.x;
+            plo[k * P + cell] = al.x;
+            if (has_y) {
+                pho[k * P + cell + 1] = ah.y;
+                plo[k * P + cell + 1] = al.y;
+            }
         }
     }
 }
@@ -863,7 +919,7 @@ struct SmemO2 {             // the tile's step constants (a copy of its TileC2)
 };
 static_assert(sizeof(SmemO2) == sizeof(TileC2), "the tile constants are copied word for word");
 
-template <bool KAHAN, bool LAM_POW2, int LIM>
+template <bool KAHAN, bool LAM_POW2, int LIM, bool VEC>
 __global__ void __launch_bounds__(NT2, 2) k_step2d_o2(Args2 A) {
     __shared__ SmemO2 S;
     extern __shared__ __align__(16) float2 g_o2[];   // [32][WR2][WP]: fp fm hp hm, then Lx Rx Ly Ry
@@ -906,8 +962,18 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d_o2(Args2 A) {
         float2 d[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) { d[k] = f2(0.f); ah[k] = f2(0.f); al[k] = f2(0.f); }
+        if (VEC && ex[0]) {   // (an even row length: the pair is inside or outside together)
+            float2 c2[4];
+            load_pair2(A, D, i, jx, kw, pp, phi, pli, ah, al, c2);
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
+            for (int k = 0; k < 4; k++) {
+                float2 b = c2[k];
+                if (nbi >= 0) b = add2(add2(b, f2(S.dn[nbi][k][0])), f2(S.dn[nbi][k][1]));
+                d[k] = add2(b, add2(ah[k], al[k]));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2 && !VEC; q++) {
             if (!ex[q]) continue;   // outside the domain or a corner: zero deviation (finite, never applied)
             const int cell = D.base + i * D.ny + jx + q;
             float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
@@ -1029,8 +1095,13 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d_o2(Args2 A) {
             ff_add(S.lf[1][k][0], S.lf[1][k][1], lane(th, qn), lane(tl, qn), rr[0], rr[1]);
         }
         const int cell = D.base + i * D.ny + jx;
-        if (own[0]) { pho[k * P + cell] = h.x; plo[k * P + cell] = l.x; }
-        if (has_y) { pho[k * P + cell + 1] = h.y; plo[k * P + cell + 1] = l.y; }
+        if (VEC) {   // (both lanes own)
+            *reinterpret_cast<float2*>(pho + k * P + cell) = h;
+            *reinterpret_cast<float2*>(plo + k * P + cell) = l;
+        } else {
+            if (own[0]) { pho[k * P + cell] = h.x; plo[k * P + cell] = l.x; }
+            if (has_y) { pho[k * P + cell + 1] = h.y; plo[k * P + cell + 1] = l.y; }
+        }
     }
 }
 
@@ -1061,6 +1132,7 @@ struct Mixed2D {
     TileD* d_tiles = nullptr;
     int fold = 16;
     int order = 1, lim = 0;        // the batch's scheme (second order: minmod 0 or MC 1)
+    bool vec = false;              // every domain has an even row length (8-byte pair accesses)
     int kstep = default_kstep();   // time steps per step launch (k_step2d2 for 2, k_step2d for 1)
     // device checkpoint of the stored state (a run starts with a fold that rebuilds frames, C and
     // the tile constants from it, so the stored state is the whole state between runs)
@@ -1148,6 +1220,9 @@ MixedState* mixed2d_attach(MixedState* m, char* err, size_t len) {
         if (it != g_tune2d.end()) { d->fold = it->second.first; if (d->order == 1) d->kstep = it->second.second; }
     }
     d->plane = off;
+    // (SHLL_2D_SCALAR_PAIRS set: per-cell accesses everywhere, the same results)
+    d->vec = std::getenv("SHLL_2D_SCALAR_PAIRS") == nullptr;
+    for (const Dom2& D : d->doms) d->vec = d->vec && D.ny % 2 == 0;
     d->nex = std::max(oex, 1L);
     d->ney = std::max(oey, 1L);
     const bool kahan = mixed_is_kahan(m);
@@ -1206,16 +1281,32 @@ int mixed2d_planes(MixedState* m, int item, MixedPlanes* out) {
 }
 
 // the second-order step kernel of the batch's variant
-static void launch_o2(bool kahan, bool pow2, int lim, int ntiles, cudaStream_t s, const Args2& A) {
+template <bool VEC>
+static void launch_o2v(bool kahan, bool pow2, int lim, int ntiles, cudaStream_t s, const Args2& A) {
     switch ((kahan ? 4 : 0) + (pow2 ? 2 : 0) + lim) {
-        case 0: k_step2d_o2<false, false, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        case 1: k_step2d_o2<false, false, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        case 2: k_step2d_o2<false, true, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        case 3: k_step2d_o2<false, true, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        case 4: k_step2d_o2<true, false, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        case 5: k_step2d_o2<true, false, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        case 6: k_step2d_o2<true, true, 0><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
-        default: k_step2d_o2<true, true, 1><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 0: k_step2d_o2<false, false, 0, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 1: k_step2d_o2<false, false, 1, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 2: k_step2d_o2<false, true, 0, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 3: k_step2d_o2<false, true, 1, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 4: k_step2d_o2<true, false, 0, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 5: k_step2d_o2<true, false, 1, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        case 6: k_step2d_o2<true, true, 0, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+        default: k_step2d_o2<true, true, 1, VEC><<<ntiles, NT2, kStepO2Smem, s>>>(A); break;
+    }
+}
+static void launch_o2(bool vec, bool kahan, bool pow2, int lim, int ntiles, cudaStream_t s, const Args2& A) {
+    if (vec) launch_o2v<true>(kahan, pow2, lim, ntiles, s, A);
+    else launch_o2v<false>(kahan, pow2, lim, ntiles, s, A);
+}
+// the first-order one-step kernel of the batch's variant
+template <bool VEC>
+static void launch_step1(bool kahan, bool pow2, int ntiles, cudaStream_t s, const Args2& A) {
+    if (kahan) {
+        if (pow2) k_step2d<true, true, VEC><<<ntiles, NTP, 0, s>>>(A);
+        else k_step2d<true, false, VEC><<<ntiles, NTP, 0, s>>>(A);
+    } else {
+        if (pow2) k_step2d<false, true, VEC><<<ntiles, NTP, 0, s>>>(A);
+        else k_step2d<false, false, VEC><<<ntiles, NTP, 0, s>>>(A);
     }
 }
 
@@ -1262,7 +1353,7 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
         const long wend = std::min<long>(s0 + d->fold, maxsteps);
         const int k = d->kstep == 2 && wend - st >= 2 ? 2 : 1;
         if (d->order == 2) {
-            launch_o2(kahan, pow2, d->lim, ntiles, s, A);
+            launch_o2(d->vec, kahan, pow2, d->lim, ntiles, s, A);
         } else if (k == 2) {
             if (kahan) {
                 if (pow2) k_step2d2<true, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
@@ -1271,12 +1362,10 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
                 if (pow2) k_step2d2<false, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
                 else k_step2d2<false, false><<<ntiles, NT2, kStep2Smem, s>>>(A);
             }
-        } else if (kahan) {
-            if (pow2) k_step2d<true, true><<<ntiles, NTP, 0, s>>>(A);
-            else k_step2d<true, false><<<ntiles, NTP, 0, s>>>(A);
+        } else if (d->vec) {
+            launch_step1<true>(kahan, pow2, ntiles, s, A);
         } else {
-            if (pow2) k_step2d<false, true><<<ntiles, NTP, 0, s>>>(A);
-            else k_step2d<false, false><<<ntiles, NTP, 0, s>>>(A);
+            launch_step1<false>(kahan, pow2, ntiles, s, A);
         }
         launches++;
         st += k;
@@ -1301,10 +1390,14 @@ static cudaError_t allow_step2_smem() {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kStep2Smem);
         if (e != cudaSuccess) return e;
     }
-    const void* ko[] = {(const void*)k_step2d_o2<false, false, 0>, (const void*)k_step2d_o2<false, false, 1>,
-                        (const void*)k_step2d_o2<false, true, 0>, (const void*)k_step2d_o2<false, true, 1>,
-                        (const void*)k_step2d_o2<true, false, 0>, (const void*)k_step2d_o2<true, false, 1>,
-                        (const void*)k_step2d_o2<true, true, 0>, (const void*)k_step2d_o2<true, true, 1>};
+    const void* ko[] = {(const void*)k_step2d_o2<false, false, 0, false>, (const void*)k_step2d_o2<false, false, 1, false>,
+                        (const void*)k_step2d_o2<false, true, 0, false>, (const void*)k_step2d_o2<false, true, 1, false>,
+                        (const void*)k_step2d_o2<true, false, 0, false>, (const void*)k_step2d_o2<true, false, 1, false>,
+                        (const void*)k_step2d_o2<true, true, 0, false>, (const void*)k_step2d_o2<true, true, 1, false>,
+                        (const void*)k_step2d_o2<false, false, 0, true>, (const void*)k_step2d_o2<false, false, 1, true>,
+                        (const void*)k_step2d_o2<false, true, 0, true>, (const void*)k_step2d_o2<false, true, 1, true>,
+                        (const void*)k_step2d_o2<true, false, 0, true>, (const void*)k_step2d_o2<true, false, 1, true>,
+                        (const void*)k_step2d_o2<true, true, 0, true>, (const void*)k_step2d_o2<true, true, 1, true>};
     for (const void* k : ko) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kStepO2Smem);
         if (e != cudaSuccess) return e;

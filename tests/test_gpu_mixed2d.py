@@ -245,3 +245,24 @@ def test_two_steps_per_launch_vs_fp64_oracle(shll, oracle, monkeypatch, prec, fo
         outs[kstep] = out
     for a, b in zip(outs[1], outs[2]):
         assert np.all(l1(a, b) <= 1e-6)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_pair_accesses_equal_per_cell_accesses(shll, order, monkeypatch):
+    # domains with even row lengths load and store their cell pairs with 8-byte accesses; the
+    # per-cell accesses of the general path give the same bits
+    def once():
+        items = [shll.params(2, order, nx=n, ny=m, precision="mixed_f64", n_steps=37, ic_kind=shll.IC_CIRCLE2D,
+                             ic_cx=0.45, ic_cy=0.55, ic_radius=0.3, ic_rho_l=8.0, ic_T_l=1.3, ic_rho_r=1.0,
+                             ic_T_r=1.0, fold_steps=16)
+                 for n, m in ((48, 40), (97, 64), (34, 34))]   # (ny <= nx: the y CFL number stays <= 0.25)
+        b = shll.Batch(items)
+        b.run()
+        out = [b.primitives(k) for k in range(len(items))]
+        b.close()
+        return out
+    pairs = once()
+    monkeypatch.setenv("SHLL_2D_SCALAR_PAIRS", "1")
+    cells = once()
+    for x, y in zip(pairs, cells):
+        assert np.array_equal(x, y)

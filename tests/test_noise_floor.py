@@ -6,7 +6,7 @@ base-c/2nd_order_base_shll.c:191-201, 438-446) amplifies a perturbation of the i
 the first-order scheme damps it.  This spread is the floor below which no arithmetic that rounds at
 FP32 scale can bring a second-order run against FP64, and the GPU tests of the mixed engine tie
 their second-order bounds to it."""
-from noise_floor import spread, spread_stepwise
+from noise_floor import spread, spread2d, spread_stepwise
 
 
 def test_second_order_spread_grows_with_the_tube():
@@ -21,3 +21,11 @@ def test_second_order_spread_grows_with_the_tube():
 
 def test_first_order_sod_tube_damps_the_same_perturbation():
     assert spread(16384, order=1)[0] < 1e-7
+
+
+def test_2d_second_order_spread():
+    # base-omp's quadrant problem with the MC limiter on 256 x 256 cells (615 steps); the same
+    # perturbation on 1024 x 1024 cells (2458 steps, measured with the FP64 GPU path) moves the
+    # result by L1(rho) 2.3e-5
+    s = spread2d(256)
+    assert 1e-8 < s[0] < 1e-7
