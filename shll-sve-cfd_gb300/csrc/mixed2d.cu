@@ -658,7 +658,7 @@ struct Smem22 {
 };
 static_assert(sizeof(TileC2) == offsetof(Smem22, recx), "the tile constants are copied word for word");
 
-template <bool KAHAN, bool LAM_POW2>
+template <bool KAHAN, bool LAM_POW2, bool VEC>
 __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
     __shared__ Smem22 S;
     extern __shared__ __align__(16) float2 g_flux2[];   // [step][16][WR2][WP]
@@ -707,8 +707,20 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
     float2 base[4], ah[4], al[4];   // deviation of the pair at the launch's start, its increments
 #pragma unroll
     for (int k = 0; k < 4; k++) { base[k] = f2(0.f); ah[k] = f2(0.f); al[k] = f2(0.f); }
+    if (VEC && ex[0]) {   // (an even row length: the pair is inside or outside together)
+        float2 c2[4];
+        load_pair2(A, D, i, jx, kw, pp, phi, pli, ah, al, c2);
 #pragma unroll
-    for (int q = 0; q < 2; q++) {
+        for (int k = 0; k < 4; k++) {
+            base[k] = c2[k];
+            if (nbi >= 0) {
+                const float* o = nbi < 4 ? S.dn[nbi][k] : S.dnd[nbi - 4][k];
+                base[k] = add2(add2(base[k], f2(o[0])), f2(o[1]));
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 2 && !VEC; q++) {
         if (!ex[q]) continue;   // outside the domain: zero deviation (finite fluxes, never applied)
         const int cell = D.base + i * D.ny + jx + q;
         float ch[4] = {0, 0, 0, 0}, cl[4] = {0, 0, 0, 0};
@@ -871,8 +883,15 @@ __global__ void __launch_bounds__(NT2, 2) k_step2d2(Args2 A) {
         const int col = jx + q - j0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            pho[k * P + cell] = lane(ah[k], q);
-            plo[k * P + cell] = lane(al[k], q);
+            if (VEC) {   // (both lanes own: written once, from lane x)
+                if (q == 0) {
+                    *reinterpret_cast<float2*>(pho + k * P + cell) = ah[k];
+                    *reinterpret_cast<float2*>(plo + k * P + cell) = al[k];
+                }
+            } else {
+                pho[k * P + cell] = lane(ah[k], q);
+                plo[k * P + cell] = lane(al[k], q);
+            }
             const float lxh = __fmul_rn(sc, S.lf[0][k][0]), lxl = __fmul_rn(sc, S.lf[0][k][1]);
             const float lyh = __fmul_rn(sc, S.lf[1][k][0]), lyl = __fmul_rn(sc, S.lf[1][k][1]);
             if (recW) {
@@ -1298,6 +1317,17 @@ static void launch_o2(bool vec, bool kahan, bool pow2, int lim, int ntiles, cuda
     if (vec) launch_o2v<true>(kahan, pow2, lim, ntiles, s, A);
     else launch_o2v<false>(kahan, pow2, lim, ntiles, s, A);
 }
+// the two-step kernel of the batch's variant
+template <bool VEC>
+static void launch_step2(bool kahan, bool pow2, int ntiles, cudaStream_t s, const Args2& A) {
+    if (kahan) {
+        if (pow2) k_step2d2<true, true, VEC><<<ntiles, NT2, kStep2Smem, s>>>(A);
+        else k_step2d2<true, false, VEC><<<ntiles, NT2, kStep2Smem, s>>>(A);
+    } else {
+        if (pow2) k_step2d2<false, true, VEC><<<ntiles, NT2, kStep2Smem, s>>>(A);
+        else k_step2d2<false, false, VEC><<<ntiles, NT2, kStep2Smem, s>>>(A);
+    }
+}
 // the first-order one-step kernel of the batch's variant
 template <bool VEC>
 static void launch_step1(bool kahan, bool pow2, int ntiles, cudaStream_t s, const Args2& A) {
@@ -1355,13 +1385,8 @@ static long issue_run2d(Mixed2D* d, MixedState* m, long maxsteps, cudaStream_t s
         if (d->order == 2) {
             launch_o2(d->vec, kahan, pow2, d->lim, ntiles, s, A);
         } else if (k == 2) {
-            if (kahan) {
-                if (pow2) k_step2d2<true, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
-                else k_step2d2<true, false><<<ntiles, NT2, kStep2Smem, s>>>(A);
-            } else {
-                if (pow2) k_step2d2<false, true><<<ntiles, NT2, kStep2Smem, s>>>(A);
-                else k_step2d2<false, false><<<ntiles, NT2, kStep2Smem, s>>>(A);
-            }
+            if (d->vec) launch_step2<true>(kahan, pow2, ntiles, s, A);
+            else launch_step2<false>(kahan, pow2, ntiles, s, A);
         } else if (d->vec) {
             launch_step1<true>(kahan, pow2, ntiles, s, A);
         } else {
@@ -1384,8 +1409,10 @@ static cudaError_t allow_step2_smem() {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev >= 64 || (done & (1ull << dev))) return e;
-    const void* ks[] = {(const void*)k_step2d2<false, false>, (const void*)k_step2d2<false, true>,
-                        (const void*)k_step2d2<true, false>, (const void*)k_step2d2<true, true>};
+    const void* ks[] = {(const void*)k_step2d2<false, false, false>, (const void*)k_step2d2<false, true, false>,
+                        (const void*)k_step2d2<true, false, false>, (const void*)k_step2d2<true, true, false>,
+                        (const void*)k_step2d2<false, false, true>, (const void*)k_step2d2<false, true, true>,
+                        (const void*)k_step2d2<true, false, true>, (const void*)k_step2d2<true, true, true>};
     for (const void* k : ks) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kStep2Smem);
         if (e != cudaSuccess) return e;

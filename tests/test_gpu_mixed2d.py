@@ -247,10 +247,12 @@ def test_two_steps_per_launch_vs_fp64_oracle(shll, oracle, monkeypatch, prec, fo
         assert np.all(l1(a, b) <= 1e-6)
 
 
-@pytest.mark.parametrize("order", [1, 2])
-def test_pair_accesses_equal_per_cell_accesses(shll, order, monkeypatch):
+@pytest.mark.parametrize("order,kstep", [(1, 1), (1, 2), (2, 1)])
+def test_pair_accesses_equal_per_cell_accesses(shll, order, kstep, monkeypatch):
     # domains with even row lengths load and store their cell pairs with 8-byte accesses; the
-    # per-cell accesses of the general path give the same bits
+    # per-cell accesses of the general path give the same bits (one and two steps per launch)
+    monkeypatch.setenv("SHLL_2D_STEPS_PER_LAUNCH", str(kstep))
+
     def once():
         items = [shll.params(2, order, nx=n, ny=m, precision="mixed_f64", n_steps=37, ic_kind=shll.IC_CIRCLE2D,
                              ic_cx=0.45, ic_cy=0.55, ic_radius=0.3, ic_rho_l=8.0, ic_T_l=1.3, ic_rho_r=1.0,
