@@ -70,7 +70,8 @@ struct TileD { int dom, ti, tj; };
 
 // one edge interface: the full flux lam*F applied by the west/south tile (side 0) and by the
 // east/north tile (side 1), four components each, as FP32 pairs (value, remainder)
-struct Edge { float r[2][4][2]; };
+struct __align__(16) Edge { float r[2][4][2]; };
+static_assert(sizeof(Edge) == 64, "an edge record is four 16-byte vectors");
 
 struct Frame2 {
     double U[4], Fx[4], Fy[4];
@@ -233,25 +234,24 @@ __device__ __forceinline__ double loadB(const Args2& A, int idx) {
 // edge correction owed to cell (i, j) by the launch whose edge buffers have index pp (0..2):
 // lam*(F of the west/south tile - F of the cell's own tile) on its west / south edge line, as an
 // FP32 pair per component
+// (each record is read as four 16-byte vectors: r[0][0..1], r[0][2..3], r[1][0..1], r[1][2..3])
+__device__ __forceinline__ void add_edge(const Edge* e, float ch[4], float cl[4]) {
+    const float4* v = reinterpret_cast<const float4*>(e);
+    const float4 a0 = v[0], a1 = v[1], b0 = v[2], b1 = v[3];
+    const float w[4][2] = {{a0.x, a0.y}, {a0.z, a0.w}, {a1.x, a1.y}, {a1.z, a1.w}};   // west/south tile
+    const float o[4][2] = {{b0.x, b0.y}, {b0.z, b0.w}, {b1.x, b1.y}, {b1.z, b1.w}};   // own tile
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        two_sum_acc(ch[k], cl[k], w[k][0]);
+        two_sum_acc(ch[k], cl[k], -o[k][0]);
+        cl[k] = __fadd_rn(cl[k], __fadd_rn(w[k][1], -o[k][1]));
+    }
+}
 __device__ __forceinline__ void edge_correction(const Args2& A, const Dom2& D, int i, int j, int pp, float ch[4],
                                                 float cl[4]) {
     for (int k = 0; k < 4; k++) { ch[k] = 0.f; cl[k] = 0.f; }
-    if (i > 0 && i % TI == 0) {
-        const Edge& e = A.ex[pp][D.ex_base + (i / TI - 1) * D.ny + j];
-        for (int k = 0; k < 4; k++) {
-            two_sum_acc(ch[k], cl[k], e.r[0][k][0]);
-            two_sum_acc(ch[k], cl[k], -e.r[1][k][0]);
-            cl[k] = __fadd_rn(cl[k], __fadd_rn(e.r[0][k][1], -e.r[1][k][1]));
-        }
-    }
-    if (j > 0 && j % TJ == 0) {
-        const Edge& e = A.ey[pp][D.ey_base + (j / TJ - 1) * D.nx + i];
-        for (int k = 0; k < 4; k++) {
-            two_sum_acc(ch[k], cl[k], e.r[0][k][0]);
-            two_sum_acc(ch[k], cl[k], -e.r[1][k][0]);
-            cl[k] = __fadd_rn(cl[k], __fadd_rn(e.r[0][k][1], -e.r[1][k][1]));
-        }
-    }
+    if (i > 0 && i % TI == 0) add_edge(&A.ex[pp][D.ex_base + (i / TI - 1) * D.ny + j], ch, cl);
+    if (j > 0 && j % TJ == 0) add_edge(&A.ey[pp][D.ey_base + (j / TJ - 1) * D.nx + i], ch, cl);
 }
 
 __device__ __forceinline__ bool on_edge_line(int i, int j) { return (i > 0 && i % TI == 0) || (j > 0 && j % TJ == 0); }
