@@ -55,18 +55,23 @@ constexpr int TI = 16;           // tile rows (x, the slow index)
 constexpr int TJ = 32;           // tile columns (y, contiguous)
 constexpr int NT = TI * TJ;      // threads of the fold kernel, one cell each
 
-struct Dom2 {
+// (the fields a step reads come first, in three aligned 16-byte groups, so that each thread loads
+// them with three vector loads)
+struct __align__(16) Dom2 {
     int base;                 // cell offset of the domain in the planes
-    int nx, ny, tiles_i, tiles_j;
+    int nx, ny;
+    int steps;                // steps of the current run
+    int tiles_j;
     int tile_base;            // first tile of this domain in the tile / frame tables
     int ex_base, ey_base;     // first edge entry of this domain in the x / y edge buffers
-    int steps;                // steps of the current run
-    double gamma, R, CV, lamx, lamy;
     float lxh, lxl, lyh, lyl; // lam_x, lam_y as FP32 pairs
+    int tiles_i;
     float alpha;              // MC limiter coefficient (second order, limiter 1)
+    double gamma, R, CV, lamx, lamy;
 };
+static_assert(offsetof(Dom2, lxh) == 32 && offsetof(Dom2, tiles_i) == 48, "step fields in 16-byte groups");
 
-struct TileD { int dom, ti, tj; };
+struct __align__(16) TileD { int dom, ti, tj; };
 
 // one edge interface: the full flux lam*F applied by the west/south tile (side 0) and by the
 // east/north tile (side 1), four components each, as FP32 pairs (value, remainder)
