@@ -268,3 +268,19 @@ def test_pair_accesses_equal_per_cell_accesses(shll, order, kstep, monkeypatch):
     cells = once()
     for x, y in zip(pairs, cells):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("limiter,ic", [(0, "four_shock"), (1, "quadrants")])
+def test_second_order_many_tiles_vs_fp64_oracle(shll, oracle, limiter, ic):
+    # 16 x 4 tiles (256 x 128 cells, 8-byte pair accesses), 150 steps: every interior tile edge and
+    # its reconciliation in use
+    nx, ny, steps = 256, 128, 150
+    cfg = oracle.make_cfg(dim=2, order=2, nx=nx, ny=ny, n_steps=steps, limiter=limiter, mc_alpha=1.25)
+    prim = oracle.ic_four_shock2d(nx, ny, 64) if ic == "four_shock" else oracle.ic_quadrants2d(nx, ny, 64)
+    _, ref, _ = oracle.run(cfg, prim)
+    kind = shll.IC_FOUR_SHOCK2D if ic == "four_shock" else shll.IC_QUADRANTS2D
+    p = shll.params(2, 2, nx=nx, ny=ny, precision="mixed_f64", n_steps=steps, limiter=limiter, mc_alpha=1.25,
+                    ic_kind=kind)
+    s, out, _, _ = run(shll, p)
+    assert s == steps
+    assert np.all(l1(out, ref) <= 1e-6), l1(out, ref)
