@@ -239,9 +239,11 @@ int shll_batch_restore(shll_batch* b);
 int shll_tube_run_static(const shll_params* p, double* d_cons, long nsteps, void* stream);
 
 /* The autotuner for a single mixed-precision context (see shll_batch_autotune).  2D (contexts and
- * batches): the fold window (16, 32, 64 or 128 steps) is timed and chosen for the whole batch and,
- * process-wide, for its size class (state format, floor(log2 of the largest domain's cells));
- * shll_tuning / shll_batch_tuning then report sweep 1, that fold window and 512-cell tiles. */
+ * batches): the fold window (16, 32, 64 or 128 steps) and, for first order, the time steps per
+ * step launch (1 or 2) are timed and chosen for the whole batch and, process-wide, for its size
+ * class (state format, scheme, floor(log2 of the largest domain's cells)); shll_tuning /
+ * shll_batch_tuning then report the steps per launch as the sweep length, that fold window and
+ * 512-cell tiles. */
 int shll_autotune(shll_ctx* ctx, int trial_steps);
 int shll_tuning(shll_ctx* ctx, int* sweep_steps, int* fold_steps, int* chunk_cells);
 
