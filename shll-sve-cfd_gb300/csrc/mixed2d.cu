@@ -230,12 +230,6 @@ struct Args2 {
     int* item_flags;
 };
 
-template <bool KAHAN>
-__device__ __forceinline__ double loadB(const Args2& A, int idx) {
-    if (KAHAN) return (double)static_cast<const float*>(A.B)[idx] + (double)A.Blo[idx];
-    return static_cast<const double*>(A.B)[idx];
-}
-
 // edge correction owed to cell (i, j) by the launch whose edge buffers have index pp (0..2):
 // lam*(F of the west/south tile - F of the cell's own tile) on its west / south edge line, as an
 // FP32 pair per component
@@ -296,13 +290,6 @@ __device__ __forceinline__ void load_pair2(const Args2& A, const Dom2& D, int i,
             }
         }
     }
-}
-
-// (th, tl) = lam * x as an FP32 pair (exact, tl = 0, when lam is an FP32 power of two: POW2)
-template <bool POW2 = false>
-__device__ __forceinline__ void lam_mul(float lh, float ll, float x, float& th, float& tl) {
-    th = __fmul_rn(lh, x);
-    tl = POW2 ? 0.f : __fadd_rn(__fmaf_rn(lh, x, -th), __fmul_rn(ll, x));
 }
 
 // ---- fold: B += P (+ the last edge corrections), new frames, C = B - U* ----

@@ -46,21 +46,7 @@ __device__ __forceinline__ void ff_sub(float ah, float al, float bh, float bl, f
     ff_add(ah, al, -bh, -bl, oh, ol);
 }
 
-__device__ __forceinline__ float minmod_f(float l, float r) {
-    if (__fmul_rn(l, r) < 0.f) return 0.f;
-    return fabsf(l) < fabsf(r) ? l : r;
-}
-// limited slope from three consecutive values: minmod (LIM = 0), or the MC limiter (LIM = 1,
-// base-omp/2nd_order_base_shll.c:316-325)
-template <int LIM>
-__device__ __forceinline__ float slope_f(float fl, float fc, float fr, float alpha) {
-    float a = __fadd_rn(fc, -fl), b = __fadd_rn(fr, -fc);
-    if (LIM == 1) return minmod_f(__fmul_rn(0.5f, __fadd_rn(fr, -fl)), __fmul_rn(alpha, minmod_f(a, b)));
-    return minmod_f(a, b);
-}
-
 __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ float fast_sqrt(float x) { return __fmul_rn(x, rsqrtf(x)); }
 
 // ---- packed FP32x2: two cells per thread, one f32x2 instruction per operation --------------
 // (__fadd2_rn / __fmul2_rn / __ffma2_rn: the sm_100-family packed FP32 instructions, each lane
